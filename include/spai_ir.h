@@ -1,0 +1,203 @@
+/* GB300-native SPAI-GMRES-IR: C ABI of libspai_ir.so.
+ *
+ * Drop-in boundary for the reference's GPU solver path (anirudhtheexe/spai-gmres-ir). Plain
+ * pointers and sizes only; no exceptions cross the boundary; every entry point returns an int
+ * (SPAI_OK or a negative SPAI_ERR_*). Numerical outcomes are reported as the reference's status
+ * enums inside spai_report, never as errors.
+ *
+ *   reference entry point (file:line)                          replaced by
+ *   cuda_gpu_spai_gmres_ir      include/bspai/cuda_ir.hpp:26-28       spai_ir_solve (F64)
+ *   fp32_cuda_spai_gmres_ir     include/bspai/fp32_cuda_spai.hpp:57-58 spai_ir_solve (F32)
+ *   cuda_construct_spai         include/bspai/cuda_spai.hpp:47        spai_create + spai_build
+ *   CudaGmresContext            include/bspai/cuda_gmres.hpp:21-36    spai_handle + spai_gmres
+ *   cuda_refine_with_preconditioner include/bspai/cuda_ir.hpp:18-22   spai_build + spai_solve
+ *   CudaCsrSpmv::multiply       include/bspai/cuda_spmv.hpp:8-20      spai_spmv
+ *   cuda_evaluate_spai_score    include/bspai/cuda_spai.hpp:48-49     spai_score
+ *   spai_status_name / gmres_status_name / ir_status_name (spai.hpp:22, gmres.hpp:21, ir.hpp:18)
+ *
+ * Ownership: the caller owns every host buffer; a handle owns all device memory it allocates.
+ * Threading: one handle per host thread; calls on a handle are stream ordered and synchronous
+ * with respect to host buffers (as the reference's "synchronous, not thread-safe" contexts).
+ */
+#ifndef SPAI_IR_H
+#define SPAI_IR_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* SpaiStatus, include/bspai/spai.hpp:10-21 (same order). */
+enum {
+    SPAI_SUCCESS = 0,
+    SPAI_NOT_ATTEMPTED = 1,
+    SPAI_INVALID_INPUT = 2,
+    SPAI_RANK_DEFICIENT = 3,
+    SPAI_NUMERICAL_FAILURE = 4,
+    SPAI_EMPTY_CANDIDATES = 5,
+    SPAI_ZERO_DENOMINATOR = 6,
+    SPAI_INVALID_SCORE = 7,
+    SPAI_NO_GROWTH = 8,
+    SPAI_ITERATION_LIMIT = 9
+};
+/* GmresStatus, include/bspai/gmres.hpp:10-20 (same order). */
+enum {
+    GMRES_SUCCESS = 0,
+    GMRES_ZERO_RHS = 1,
+    GMRES_EXACT_INITIAL_SOLUTION = 2,
+    GMRES_INVALID_INPUT = 3,
+    GMRES_ZERO_PRECONDITIONED_RHS = 4,
+    GMRES_BREAKDOWN = 5,
+    GMRES_ITERATION_LIMIT = 6,
+    GMRES_NONCONVERGENCE = 7,
+    GMRES_NUMERICAL_FAILURE = 8
+};
+/* IrStatus, include/bspai/ir.hpp:9-17 (same order). */
+enum {
+    IR_SUCCESS = 0,
+    IR_INVALID_INPUT = 1,
+    IR_CONSTRUCTION_FAILURE = 2,
+    IR_INNER_FAILURE = 3,
+    IR_STAGNATION = 4,
+    IR_ITERATION_LIMIT = 5,
+    IR_NUMERICAL_FAILURE = 6
+};
+
+/* API return codes (the reference throws std::runtime_error / std::invalid_argument). */
+enum {
+    SPAI_OK = 0,
+    SPAI_ERR_ARGUMENT = -1,  /* invalid_argument: bad sizes, non-canonical CSR, bad options */
+    SPAI_ERR_CUDA = -2,      /* runtime_error from the CUDA runtime (message: spai_last_error) */
+    SPAI_ERR_WORKSPACE = -3, /* a SPAI column exceeded the largest fit workspace */
+    SPAI_ERR_TIMEOUT = -4,   /* a bounded device wait gave up */
+    SPAI_ERR_NOT_BUILT = -5, /* spai_solve before a successful spai_build */
+    SPAI_ERR_UNSUPPORTED = -6
+};
+
+/* Precision forms. F64 is the drop-in for gpu_fp64_ir; F32 for gpu_fp32_ir; MIXED builds the
+ * SPAI and runs GMRES in binary32 with binary64 refinement residual, update and norms. */
+enum { SPAI_PREC_F64 = 0, SPAI_PREC_F32 = 1, SPAI_PREC_MIXED = 2 };
+
+/* Option flags. */
+enum {
+    SPAI_FLAG_NO_GRAPH = 1 /* run the refinement loop with host launches instead of one graph */
+};
+
+/* Canonical CSR on the host (row_offsets[n+1], sorted col_indices[nnz], no stored zeros), the
+ * layout of CsrMatrix (include/bspai/cpu.hpp:17-43) with 64-bit indices. */
+typedef struct {
+    int64_t n;
+    int64_t nnz;
+    const int64_t *row_offsets;
+    const int64_t *col_indices;
+    const double *values;
+} spai_csr;
+
+/* SpaiOptions + GmresOptions + IrOptions (spai.hpp:24-28, gmres.hpp:23-26, ir.hpp:20-24). */
+typedef struct {
+    double epsilon;       /* SPAI column residual target (reference default 0.3) */
+    int64_t alpha;        /* growth budget per column (default 5; the CLI uses ceil(n/8)) */
+    int64_t beta;         /* maximum candidates added per growth (default 8) */
+    double tau;           /* inner GMRES tolerance; 0 = 1e-8 (F64) or 1e-4 (F32, MIXED) */
+    int64_t innercap;     /* GMRES iteration cap; 0 = n */
+    int64_t outercap;     /* refinement correction cap, <= 20 */
+    double be_tolerance;  /* outer stop on normwise backward error; 0 = 10u (2^-53 or 2^-24) */
+    int32_t precision;    /* SPAI_PREC_* */
+    int32_t flags;        /* SPAI_FLAG_* */
+} spai_options;
+
+/* Result summary (IrResult/IrDiagnostics/SpaiResult fields, ir.hpp:26-56). */
+typedef struct {
+    int32_t ir_status;         /* IR_* */
+    int32_t spai_status;       /* SPAI_* (overall construction status) */
+    int32_t gmres_status;      /* GMRES_* of the last inner solve, -1 if none */
+    int32_t converged;
+    int64_t outer_steps;
+    int64_t inner_attempts;
+    int64_t inner_iterations;  /* summed over inner solves */
+    int64_t nnz_p;
+    int64_t first_failed_column; /* -1 when every column succeeded */
+    double backward_error;     /* normwise ||r||_inf / (||A||_inf ||x||_inf + ||b||_inf) */
+    double componentwise_backward_error;
+    double residual_inf;
+    double forward_error;      /* ||x - reference||_inf / ||reference||_inf, NaN without one */
+    double spai_ms;            /* device time of the SPAI construction */
+    double solve_ms;           /* device time of the refinement loop */
+    int64_t spai_fits;
+    int64_t spai_growths;
+    int64_t spai_overflow_columns; /* columns refit in the large-workspace pass */
+    int64_t kernel_launches;   /* kernels launched by the last build/solve call */
+} spai_report;
+
+typedef struct spai_handle_s spai_handle;
+
+/* Fill *opt with the reference defaults for a precision (alpha 5, beta 8, epsilon 0.3,
+ * outercap 20, innercap 0, tau and be_tolerance 0 = precision defaults). */
+int spai_default_options(spai_options *opt, int32_t precision);
+
+const char *spai_status_name(int32_t status);  /* spai.cpp:247-270 names */
+const char *gmres_status_name(int32_t status); /* gmres.cpp:64-85 names */
+const char *ir_status_name(int32_t status);    /* ir.cpp:59-76 names */
+const char *spai_last_error(void);             /* message of the last SPAI_ERR_* on this thread */
+
+/* Upload A (host CSR, canonical) to `device`, on `stream` (cudaStream_t, may be NULL). */
+int spai_create(const spai_csr *a, int32_t precision, int device, void *stream, spai_handle **out);
+int spai_destroy(spai_handle *h);
+
+/* Adaptive SPAI construction on the device (cuda_construct_spai). rep may be NULL. */
+int spai_build(spai_handle *h, const spai_options *opt, spai_report *rep);
+
+/* Refinement solve with the built preconditioner; host b, host x (cuda_refine_with_preconditioner
+ * semantics; x0 = P b). reference may be NULL. */
+int spai_solve(spai_handle *h, const double *b, double *x, const double *reference,
+               const spai_options *opt, spai_report *rep);
+/* Same with device pointers (b, x resident in HBM; no host copies). */
+int spai_solve_device(spai_handle *h, const double *d_b, double *d_x, const spai_options *opt,
+                      spai_report *rep);
+
+/* One call: create, build, solve, destroy (cuda_gpu_spai_gmres_ir / fp32_cuda_spai_gmres_ir). */
+int spai_ir_solve(const spai_csr *a, const double *b, double *x, const double *reference,
+                  const spai_options *opt, spai_report *rep, void *stream);
+
+/* Built preconditioner P (CSR). Pass NULL arrays to query nnz only. */
+int spai_get_preconditioner(spai_handle *h, int64_t *nnz, int64_t *row_offsets,
+                            int64_t *col_indices, double *values);
+/* Per-column construction metadata (SpaiColumn, spai.hpp:44-55); arrays of length n, any NULL. */
+int spai_get_columns(spai_handle *h, int32_t *status, int32_t *fits, int32_t *growths,
+                     int32_t *score_clamps, double *residual, double *scaling);
+/* Solved pattern/coefficients of column k (N(:,k)); returns the pattern size via *q. */
+int spai_get_column(spai_handle *h, int64_t k, int64_t *q, int64_t *pattern, double *coefficients);
+
+/* y = M x on the device in the handle's inner precision; which: 0 = A, 1 = P (CudaCsrSpmv). */
+int spai_spmv(spai_handle *h, int32_t which, const double *x, double *y);
+
+/* One left-preconditioned GMRES solve P A d = P rhs with x0 = 0 (CudaGmresContext::solve).
+ * out_status = GMRES_*, out_iterations, out_relative = recomputed preconditioned residual. */
+int spai_gmres(spai_handle *h, const double *rhs, double *x, double tau, int64_t cap,
+               int32_t *out_status, int64_t *out_iterations, double *out_relative);
+
+/* Score guard KAT on the device (cuda_evaluate_spai_score). out = {status, score, clamped}. */
+int spai_score(int32_t precision, double rsq, double dot, double den, double *out);
+
+/* Batched: `count` independent systems, each with its own SPAI, solved together (one build pass
+ * and one refinement loop over all systems). b[i], x[i] are host vectors of systems[i].n. */
+int spai_ir_solve_batched(int64_t count, const spai_csr *systems, const double *const *b,
+                          double *const *x, const spai_options *opt, spai_report *reports,
+                          void *stream);
+
+/* Adjoint of x = A^{-1} b for nrhs right-hand sides (column-major n x nrhs): solves
+ * A^T lambda = dLdx by GMRES right-preconditioned with P^T (same SPAI, no rebuild), then
+ * dLdb = lambda and dLdA[e] = -sum_r lambda_r[i] x_r[j] over A's pattern (e = (i, j)). */
+int spai_adjoint(spai_handle *h, int64_t nrhs, const double *x, const double *dLdx,
+                 double *dLdb, double *dLdA_values, const spai_options *opt, spai_report *rep);
+
+/* Host builds of the device hypot used by the SPAI fits (parity tests). */
+double spai_hypot(double a, double b);
+float spai_hypotf(float a, float b);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

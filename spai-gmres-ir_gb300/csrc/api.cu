@@ -1,0 +1,778 @@
+// C ABI of libspai_ir.so: handle management, uploads, SPAI build, refinement solves.
+// The entry points and their reference counterparts are listed in include/spai_ir.h.
+#include "krylov_kernels.cuh"
+#include "spai_ir.h"
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <type_traits>
+#include <string>
+#include <vector>
+
+using namespace spai;
+
+namespace spai_api {
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string &msg) {
+    g_last_error = msg;
+    return code;
+}
+
+// int64 host CSR -> int32 device CSR (upload once, convert on the device).
+__global__ void narrow_kernel(long long count, const long long *src, int *dst) {
+    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < count;
+         i += static_cast<long long>(gridDim.x) * blockDim.x)
+        dst[i] = static_cast<int>(src[i]);
+}
+template <class TD, class TS>
+__global__ void convert_kernel(long long count, const TS *src, TD *dst) {
+    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < count;
+         i += static_cast<long long>(gridDim.x) * blockDim.x)
+        dst[i] = static_cast<TD>(src[i]);
+}
+
+// Canonical CSR check (src/cuda_spai.cu:452-470): offsets monotone from 0 to nnz, columns in
+// range and strictly increasing per row, values finite and nonzero.
+std::string canonical_error(const spai_csr *a) {
+    if (!a || a->n <= 0 || a->nnz < 0 || !a->row_offsets || (a->nnz > 0 && (!a->col_indices || !a->values)))
+        return "CSR pointers/sizes invalid";
+    if (a->n > INT_MAX - 1 || a->nnz > INT_MAX - 1)
+        return "matrix exceeds 32-bit device index range";
+    if (a->row_offsets[0] != 0 || a->row_offsets[a->n] != a->nnz)
+        return "row offsets must run from 0 to nnz";
+    for (int64_t r = 0; r < a->n; ++r) {
+        const int64_t b = a->row_offsets[r], e = a->row_offsets[r + 1];
+        if (b > e)
+            return "row offsets must be nondecreasing";
+        for (int64_t t = b; t < e; ++t) {
+            const int64_t c = a->col_indices[t];
+            if (c < 0 || c >= a->n)
+                return "column index outside matrix";
+            if (t > b && a->col_indices[t - 1] >= c)
+                return "column indices must be strictly increasing within a row";
+            if (!std::isfinite(a->values[t]) || a->values[t] == 0)
+                return "values must be finite and nonzero (canonical CSR)";
+        }
+    }
+    return "";
+}
+
+int sm_count(int device) {
+    int sms = 0;
+    SPAI_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+    return sms;
+}
+
+struct EventTimer {
+    cudaEvent_t a = nullptr, b = nullptr;
+    cudaStream_t st;
+    explicit EventTimer(cudaStream_t s) : st(s) {
+        SPAI_CUDA(cudaEventCreate(&a));
+        SPAI_CUDA(cudaEventCreate(&b));
+        SPAI_CUDA(cudaEventRecord(a, st));
+    }
+    double stop() {
+        SPAI_CUDA(cudaEventRecord(b, st));
+        SPAI_CUDA(cudaEventSynchronize(b));
+        float ms = 0;
+        SPAI_CUDA(cudaEventElapsedTime(&ms, a, b));
+        return ms;
+    }
+    ~EventTimer() {
+        if (a)
+            cudaEventDestroy(a);
+        if (b)
+            cudaEventDestroy(b);
+    }
+};
+} // namespace spai_api
+using namespace spai_api;
+
+struct spai_handle_s {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int precision = SPAI_PREC_F64;
+    int n = 0, nnz = 0, sms = 0;
+    DeviceArena mat, build, solve, scratch;
+    DeviceCsr<double> a64;
+    DeviceCsr<float> a32;
+    SpaiOutput<double> s64;
+    SpaiOutput<float> s32;
+    bool built = false;
+    int spai_status = SPAI_NOT_ATTEMPTED;
+    int *pinned = nullptr;
+    IrEngine<double, double> e64;
+    IrEngine<float, double> emix;
+    IrEngine<float, float> e32;
+    int engine_cap = -1;
+    double spai_ms = 0;
+    long long spai_launches = 0;
+
+    bool inner_f32() const {
+        return precision != SPAI_PREC_F64;
+    }
+    ~spai_handle_s() {
+        if (stream)
+            cudaStreamSynchronize(stream);
+        if (pinned)
+            cudaFreeHost(pinned);
+        if (own_stream && stream)
+            cudaStreamDestroy(stream);
+    }
+};
+
+namespace spai_api {
+
+void fill_defaults(spai_options *o, int32_t precision) {
+    o->epsilon = 0.3;
+    o->alpha = 5;
+    o->beta = 8;
+    o->tau = 0;
+    o->innercap = 0;
+    o->outercap = 20;
+    o->be_tolerance = 0;
+    o->precision = precision;
+    o->flags = 0;
+}
+
+double inner_tau(const spai_options &o) {
+    if (o.tau > 0)
+        return o.tau;
+    return o.precision == SPAI_PREC_F64 ? 1e-8 : 1e-4;
+}
+double be_tol(const spai_options &o) {
+    if (o.be_tolerance > 0)
+        return o.be_tolerance;
+    return o.precision == SPAI_PREC_F32 ? 10 * std::ldexp(1.0, -24) : 10 * std::ldexp(1.0, -53);
+}
+
+void clear_report(spai_report *r) {
+    std::memset(r, 0, sizeof(*r));
+    r->ir_status = IR_INVALID_INPUT;
+    r->spai_status = SPAI_NOT_ATTEMPTED;
+    r->gmres_status = -1;
+    r->first_failed_column = -1;
+    r->backward_error = NAN;
+    r->componentwise_backward_error = NAN;
+    r->residual_inf = NAN;
+    r->forward_error = NAN;
+}
+
+void ensure_engine(spai_handle *h, int cap) {
+    if (h->engine_cap == cap)
+        return;
+    h->solve.reset();
+    const int sms = h->sms;
+    if (h->precision == SPAI_PREC_F64)
+        h->e64.setup(h->solve, h->a64, h->a64, h->s64.p, cap, sms);
+    else if (h->precision == SPAI_PREC_MIXED)
+        h->emix.setup(h->solve, h->a64, h->a32, h->s32.p, cap, sms);
+    else
+        h->e32.setup(h->solve, h->a32, h->a32, h->s32.p, cap, sms);
+    h->engine_cap = cap;
+}
+
+template <class E> void read_ctl(spai_handle *h, E &e, Ctl &c) {
+    SPAI_CUDA(cudaMemcpyAsync(&c, e.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, h->stream));
+    SPAI_CUDA(cudaStreamSynchronize(h->stream));
+}
+
+void fill_from_ctl(const Ctl &c, spai_report *rep) {
+    rep->ir_status = c.ir_status < 0 ? IR_ITERATION_LIMIT : c.ir_status;
+    rep->converged = c.ir_status == IR_SUCCESS;
+    rep->outer_steps = c.outer_steps;
+    rep->inner_attempts = c.inner_attempts;
+    rep->inner_iterations = c.inner_iterations_total;
+    rep->gmres_status = c.last_gmres_status;
+    rep->backward_error = c.be;
+    rep->componentwise_backward_error = c.cbe;
+    rep->residual_inf = c.rinf;
+}
+
+// Validation of IrOptions against the matrix (src/ir.cpp:41-55): failures are reported as
+// IrStatus::invalid_input, not as API errors.
+bool options_valid(const spai_handle *h, const spai_options &o) {
+    return o.outercap >= 0 && o.outercap <= 20 && o.innercap >= 0 && o.innercap <= h->n &&
+           std::isfinite(inner_tau(o)) && inner_tau(o) > 0 && o.alpha >= 0 && o.beta >= 0;
+}
+
+// Solve with device vectors b, x (binary64). Returns SPAI_OK and fills rep.
+int solve_device_impl(spai_handle *h, const double *d_b, double *d_x, const spai_options &o,
+                      spai_report *rep) {
+    if (!h->built)
+        return fail(SPAI_ERR_NOT_BUILT, "spai_solve before a successful spai_build");
+    rep->spai_status = h->spai_status;
+    rep->spai_ms = h->spai_ms;
+    if (h->spai_status != SPAI_SUCCESS) {
+        rep->ir_status = IR_CONSTRUCTION_FAILURE;
+        return SPAI_OK;
+    }
+    if (!options_valid(h, o)) {
+        rep->ir_status = IR_INVALID_INPUT;
+        return SPAI_OK;
+    }
+    const int cap = o.innercap == 0 ? h->n : static_cast<int>(o.innercap);
+    ensure_engine(h, cap);
+    SolveSettings s;
+    s.cap = cap;
+    s.outer_cap = static_cast<int>(o.outercap);
+    s.tau = inner_tau(o);
+    s.be_tol = be_tol(o);
+    s.scale_rhs = h->precision == SPAI_PREC_MIXED;
+    s.accept_every = h->precision == SPAI_PREC_F32;
+    s.use_graph = (o.flags & SPAI_FLAG_NO_GRAPH) == 0;
+    EventTimer timer(h->stream);
+    Ctl c{};
+    if (h->precision == SPAI_PREC_F64) {
+        h->e64.solve(h->stream, d_b, d_x, s, h->pinned);
+        rep->solve_ms = timer.stop();
+        read_ctl(h, h->e64, c);
+        rep->kernel_launches = h->e64.launches;
+    } else if (h->precision == SPAI_PREC_MIXED) {
+        h->emix.solve(h->stream, d_b, d_x, s, h->pinned);
+        rep->solve_ms = timer.stop();
+        read_ctl(h, h->emix, c);
+        rep->kernel_launches = h->emix.launches;
+    } else {
+        // binary32 drop-in: b rounded to binary32, refinement in binary32.
+        h->scratch.reset();
+        float *bf = h->scratch.alloc<float>(h->n);
+        float *xf = h->scratch.alloc<float>(h->n);
+        convert_kernel<float, double><<<grid_for(h->n, 256, h->sms * 8), 256, 0, h->stream>>>(h->n, d_b, bf);
+        SPAI_LAUNCH("convert_kernel");
+        h->e32.solve(h->stream, bf, xf, s, h->pinned);
+        convert_kernel<double, float><<<grid_for(h->n, 256, h->sms * 8), 256, 0, h->stream>>>(h->n, xf, d_x);
+        SPAI_LAUNCH("convert_kernel");
+        rep->solve_ms = timer.stop();
+        read_ctl(h, h->e32, c);
+        rep->kernel_launches = h->e32.launches + 2;
+    }
+    fill_from_ctl(c, rep);
+    rep->nnz_p = h->precision == SPAI_PREC_F64 ? h->s64.p.nnz : h->s32.p.nnz;
+    return SPAI_OK;
+}
+
+#define API_BEGIN try {
+#define API_END                                                                                    \
+    }                                                                                              \
+    catch (const spai::ArgumentError &e) {                                                         \
+        return fail(SPAI_ERR_ARGUMENT, e.what());                                                  \
+    }                                                                                              \
+    catch (const spai::WorkspaceError &e) {                                                        \
+        return fail(SPAI_ERR_WORKSPACE, e.what());                                                 \
+    }                                                                                              \
+    catch (const std::exception &e) {                                                              \
+        return fail(SPAI_ERR_CUDA, e.what());                                                      \
+    }
+
+} // namespace spai_api
+
+extern "C" {
+
+int spai_default_options(spai_options *opt, int32_t precision) {
+    if (!opt || precision < 0 || precision > 2)
+        return fail(SPAI_ERR_ARGUMENT, "spai_default_options: bad arguments");
+    fill_defaults(opt, precision);
+    return SPAI_OK;
+}
+
+const char *spai_status_name(int32_t s) {
+    static const char *names[] = {"success",          "not_attempted",     "invalid_input",
+                                  "rank_deficient",   "numerical_failure", "empty_candidates",
+                                  "zero_denominator", "invalid_score",     "no_growth",
+                                  "iteration_limit"};
+    return (s >= 0 && s < 10) ? names[s] : "unknown";
+}
+const char *gmres_status_name(int32_t s) {
+    static const char *names[] = {"success",         "zero_rhs",       "exact_initial_solution",
+                                  "invalid_input",   "zero_preconditioned_rhs",
+                                  "breakdown",       "iteration_limit", "nonconvergence",
+                                  "numerical_failure"};
+    return (s >= 0 && s < 9) ? names[s] : "unknown";
+}
+const char *ir_status_name(int32_t s) {
+    static const char *names[] = {"success",    "invalid_input",   "construction_failure",
+                                  "inner_failure", "stagnation",   "iteration_limit",
+                                  "numerical_failure"};
+    return (s >= 0 && s < 7) ? names[s] : "unknown";
+}
+const char *spai_last_error(void) {
+    return g_last_error.c_str();
+}
+
+int spai_create(const spai_csr *a, int32_t precision, int device, void *stream, spai_handle **out) {
+    API_BEGIN
+    if (!out || precision < 0 || precision > 2)
+        return fail(SPAI_ERR_ARGUMENT, "spai_create: bad arguments");
+    *out = nullptr;
+    const std::string why = canonical_error(a);
+    if (!why.empty())
+        return fail(SPAI_ERR_ARGUMENT, "spai_create: " + why);
+    SPAI_CUDA(cudaSetDevice(device));
+    std::unique_ptr<spai_handle> h(new spai_handle());
+    h->device = device;
+    h->precision = precision;
+    h->n = static_cast<int>(a->n);
+    h->nnz = static_cast<int>(a->nnz);
+    h->sms = sm_count(device);
+    if (stream) {
+        h->stream = static_cast<cudaStream_t>(stream);
+    } else {
+        SPAI_CUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+        h->own_stream = true;
+    }
+    SPAI_CUDA(cudaMallocHost(&h->pinned, 64));
+    const int n = h->n, nnz = h->nnz;
+    h->a64.n = n;
+    h->a64.nnz = nnz;
+    h->a64.rp = h->mat.alloc<int>(n + 1);
+    h->a64.ci = h->mat.alloc<int>(nnz);
+    h->a64.val = h->mat.alloc<double>(nnz);
+    long long *tmp = h->scratch.alloc<long long>(std::max(n + 1, nnz));
+    cudaStream_t st = h->stream;
+    SPAI_CUDA(cudaMemcpyAsync(tmp, a->row_offsets, sizeof(long long) * (n + 1), cudaMemcpyHostToDevice, st));
+    narrow_kernel<<<grid_for(n + 1, 256, h->sms * 8), 256, 0, st>>>(n + 1, tmp, h->a64.rp);
+    SPAI_LAUNCH("narrow_kernel");
+    if (nnz > 0) {
+        SPAI_CUDA(cudaMemcpyAsync(tmp, a->col_indices, sizeof(long long) * nnz, cudaMemcpyHostToDevice, st));
+        narrow_kernel<<<grid_for(nnz, 256, h->sms * 8), 256, 0, st>>>(nnz, tmp, h->a64.ci);
+        SPAI_LAUNCH("narrow_kernel");
+        SPAI_CUDA(cudaMemcpyAsync(h->a64.val, a->values, sizeof(double) * nnz, cudaMemcpyHostToDevice, st));
+    }
+    if (precision != SPAI_PREC_F64) {
+        h->a32.n = n;
+        h->a32.nnz = nnz;
+        h->a32.rp = h->a64.rp;
+        h->a32.ci = h->a64.ci;
+        h->a32.val = h->mat.alloc<float>(nnz);
+        convert_kernel<float, double><<<grid_for(nnz, 256, h->sms * 8), 256, 0, st>>>(nnz, h->a64.val, h->a32.val);
+        SPAI_LAUNCH("convert_kernel");
+    }
+    SPAI_CUDA(cudaStreamSynchronize(st));
+    *out = h.release();
+    return SPAI_OK;
+    API_END
+}
+
+int spai_destroy(spai_handle *h) {
+    API_BEGIN
+    if (!h)
+        return SPAI_OK;
+    SPAI_CUDA(cudaSetDevice(h->device));
+    delete h;
+    return SPAI_OK;
+    API_END
+}
+
+int spai_build(spai_handle *h, const spai_options *opt, spai_report *rep) {
+    API_BEGIN
+    if (!h || !opt)
+        return fail(SPAI_ERR_ARGUMENT, "spai_build: null argument");
+    spai_report local;
+    if (!rep)
+        rep = &local;
+    clear_report(rep);
+    SPAI_CUDA(cudaSetDevice(h->device));
+    h->built = false;
+    h->engine_cap = -1;
+    h->build.reset();
+    SpaiParams prm;
+    prm.epsilon = opt->epsilon;
+    prm.alpha = opt->alpha;
+    prm.beta = static_cast<int>(std::min<int64_t>(opt->beta, INT_MAX));
+    if (opt->alpha < 0 || opt->beta < 0)
+        return fail(SPAI_ERR_ARGUMENT, "spai_build: alpha and beta must be nonnegative");
+    EventTimer timer(h->stream);
+    int status, first, overflow;
+    long long fits, growths, launches, nnzp;
+    if (h->precision == SPAI_PREC_F64) {
+        SpaiBuilder<double>::construct(h->a64, prm, h->stream, h->s64, h->build);
+        status = h->s64.status;
+        first = h->s64.first_failed;
+        fits = h->s64.fits;
+        growths = h->s64.growths;
+        overflow = h->s64.overflow_columns;
+        launches = h->s64.launches;
+        nnzp = h->s64.p.nnz;
+    } else {
+        SpaiBuilder<float>::construct(h->a32, prm, h->stream, h->s32, h->build);
+        status = h->s32.status;
+        first = h->s32.first_failed;
+        fits = h->s32.fits;
+        growths = h->s32.growths;
+        overflow = h->s32.overflow_columns;
+        launches = h->s32.launches;
+        nnzp = h->s32.p.nnz;
+    }
+    h->spai_ms = timer.stop();
+    h->spai_status = status;
+    h->built = true;
+    rep->spai_status = status;
+    rep->first_failed_column = first;
+    rep->spai_fits = fits;
+    rep->spai_growths = growths;
+    rep->spai_overflow_columns = overflow;
+    rep->nnz_p = nnzp;
+    rep->spai_ms = h->spai_ms;
+    rep->kernel_launches = launches;
+    rep->ir_status = status == SPAI_SUCCESS ? IR_INVALID_INPUT : IR_CONSTRUCTION_FAILURE;
+    return SPAI_OK;
+    API_END
+}
+
+int spai_solve_device(spai_handle *h, const double *d_b, double *d_x, const spai_options *opt,
+                      spai_report *rep) {
+    API_BEGIN
+    if (!h || !d_b || !d_x || !opt)
+        return fail(SPAI_ERR_ARGUMENT, "spai_solve_device: null argument");
+    spai_report local;
+    if (!rep)
+        rep = &local;
+    clear_report(rep);
+    SPAI_CUDA(cudaSetDevice(h->device));
+    return solve_device_impl(h, d_b, d_x, *opt, rep);
+    API_END
+}
+
+int spai_solve(spai_handle *h, const double *b, double *x, const double *reference,
+               const spai_options *opt, spai_report *rep) {
+    API_BEGIN
+    if (!h || !b || !x || !opt)
+        return fail(SPAI_ERR_ARGUMENT, "spai_solve: null argument");
+    spai_report local;
+    if (!rep)
+        rep = &local;
+    clear_report(rep);
+    SPAI_CUDA(cudaSetDevice(h->device));
+    const int n = h->n;
+    for (int i = 0; i < n; ++i)
+        if (!std::isfinite(b[i]) || (reference && !std::isfinite(reference[i]))) {
+            rep->ir_status = IR_INVALID_INPUT; // src/ir.cpp:48-53
+            rep->spai_status = h->spai_status;
+            return SPAI_OK;
+        }
+    h->scratch.reset();
+    double *db = h->scratch.alloc<double>(n);
+    double *dx = h->scratch.alloc<double>(n);
+    SPAI_CUDA(cudaMemcpyAsync(db, b, sizeof(double) * n, cudaMemcpyHostToDevice, h->stream));
+    const int rc = solve_device_impl(h, db, dx, *opt, rep);
+    if (rc != SPAI_OK)
+        return rc;
+    if (rep->ir_status != IR_CONSTRUCTION_FAILURE && rep->ir_status != IR_INVALID_INPUT) {
+        SPAI_CUDA(cudaMemcpyAsync(x, dx, sizeof(double) * n, cudaMemcpyDeviceToHost, h->stream));
+        SPAI_CUDA(cudaStreamSynchronize(h->stream));
+        if (reference) {
+            double rinf = 0, einf = 0;
+            bool overflow = false;
+            for (int i = 0; i < n; ++i) {
+                rinf = std::max(rinf, std::fabs(reference[i]));
+                const double e = std::fabs(x[i] - reference[i]);
+                overflow |= !std::isfinite(e);
+                einf = std::max(einf, e);
+            }
+            rep->forward_error = rinf == 0 ? einf : einf / rinf;
+            if (overflow || !std::isfinite(rep->forward_error))
+                rep->forward_error = INFINITY;
+        }
+    }
+    return SPAI_OK;
+    API_END
+}
+
+int spai_ir_solve(const spai_csr *a, const double *b, double *x, const double *reference,
+                  const spai_options *opt, spai_report *rep, void *stream) {
+    API_BEGIN
+    if (!opt || !b || !x)
+        return fail(SPAI_ERR_ARGUMENT, "spai_ir_solve: null argument");
+    spai_report local;
+    if (!rep)
+        rep = &local;
+    clear_report(rep);
+    spai_handle *h = nullptr;
+    int rc = spai_create(a, opt->precision, 0, stream, &h);
+    if (rc != SPAI_OK)
+        return rc;
+    std::unique_ptr<spai_handle, int (*)(spai_handle *)> guard(h, spai_destroy);
+    if (!options_valid(h, *opt)) {
+        rep->ir_status = IR_INVALID_INPUT;
+        return SPAI_OK;
+    }
+    for (int64_t i = 0; i < a->n; ++i)
+        if (!std::isfinite(b[i]) || (reference && !std::isfinite(reference[i]))) {
+            rep->ir_status = IR_INVALID_INPUT;
+            return SPAI_OK;
+        }
+    spai_report brep;
+    rc = spai_build(h, opt, &brep);
+    if (rc != SPAI_OK)
+        return rc;
+    rc = spai_solve(h, b, x, reference, opt, rep);
+    rep->spai_fits = brep.spai_fits;
+    rep->spai_growths = brep.spai_growths;
+    rep->spai_overflow_columns = brep.spai_overflow_columns;
+    rep->first_failed_column = brep.first_failed_column;
+    rep->kernel_launches += brep.kernel_launches;
+    return rc;
+    API_END
+}
+
+int spai_get_preconditioner(spai_handle *h, int64_t *nnz, int64_t *row_offsets,
+                            int64_t *col_indices, double *values) {
+    API_BEGIN
+    if (!h || !nnz)
+        return fail(SPAI_ERR_ARGUMENT, "spai_get_preconditioner: null argument");
+    if (!h->built)
+        return fail(SPAI_ERR_NOT_BUILT, "no preconditioner built");
+    const bool f64 = h->precision == SPAI_PREC_F64;
+    const int n = h->n;
+    const int pn = f64 ? h->s64.p.nnz : h->s32.p.nnz;
+    *nnz = pn;
+    if (!row_offsets && !col_indices && !values)
+        return SPAI_OK;
+    std::vector<int> rp(n + 1), ci(pn);
+    const int *drp = f64 ? h->s64.p.rp : h->s32.p.rp;
+    const int *dci = f64 ? h->s64.p.ci : h->s32.p.ci;
+    if (!drp) {
+        std::fill(rp.begin(), rp.end(), 0);
+    } else {
+        SPAI_CUDA(cudaMemcpy(rp.data(), drp, sizeof(int) * (n + 1), cudaMemcpyDeviceToHost));
+        if (pn)
+            SPAI_CUDA(cudaMemcpy(ci.data(), dci, sizeof(int) * pn, cudaMemcpyDeviceToHost));
+    }
+    if (row_offsets)
+        for (int i = 0; i <= n; ++i)
+            row_offsets[i] = rp[i];
+    if (col_indices)
+        for (int i = 0; i < pn; ++i)
+            col_indices[i] = ci[i];
+    if (values && pn) {
+        if (f64) {
+            SPAI_CUDA(cudaMemcpy(values, h->s64.p.val, sizeof(double) * pn, cudaMemcpyDeviceToHost));
+        } else {
+            std::vector<float> v(pn);
+            SPAI_CUDA(cudaMemcpy(v.data(), h->s32.p.val, sizeof(float) * pn, cudaMemcpyDeviceToHost));
+            for (int i = 0; i < pn; ++i)
+                values[i] = v[i];
+        }
+    }
+    return SPAI_OK;
+    API_END
+}
+
+int spai_get_columns(spai_handle *h, int32_t *status, int32_t *fits, int32_t *growths,
+                     int32_t *score_clamps, double *residual, double *scaling) {
+    API_BEGIN
+    if (!h)
+        return fail(SPAI_ERR_ARGUMENT, "spai_get_columns: null handle");
+    if (!h->built)
+        return fail(SPAI_ERR_NOT_BUILT, "no preconditioner built");
+    const int n = h->n;
+    const bool f64 = h->precision == SPAI_PREC_F64;
+    auto get_i = [&](int32_t *dst, const int *src) {
+        if (dst && src)
+            SPAI_CUDA(cudaMemcpy(dst, src, sizeof(int) * n, cudaMemcpyDeviceToHost));
+    };
+    if (f64) {
+        get_i(status, h->s64.col_status);
+        get_i(fits, h->s64.col_fits);
+        get_i(growths, h->s64.col_growths);
+        get_i(score_clamps, h->s64.col_clamps);
+        if (residual && h->s64.col_residual)
+            SPAI_CUDA(cudaMemcpy(residual, h->s64.col_residual, sizeof(double) * n, cudaMemcpyDeviceToHost));
+        if (scaling && h->s64.d)
+            SPAI_CUDA(cudaMemcpy(scaling, h->s64.d, sizeof(double) * n, cudaMemcpyDeviceToHost));
+    } else {
+        get_i(status, h->s32.col_status);
+        get_i(fits, h->s32.col_fits);
+        get_i(growths, h->s32.col_growths);
+        get_i(score_clamps, h->s32.col_clamps);
+        std::vector<float> v(n);
+        if (residual && h->s32.col_residual) {
+            SPAI_CUDA(cudaMemcpy(v.data(), h->s32.col_residual, sizeof(float) * n, cudaMemcpyDeviceToHost));
+            for (int i = 0; i < n; ++i)
+                residual[i] = v[i];
+        }
+        if (scaling && h->s32.d) {
+            SPAI_CUDA(cudaMemcpy(v.data(), h->s32.d, sizeof(float) * n, cudaMemcpyDeviceToHost));
+            for (int i = 0; i < n; ++i)
+                scaling[i] = v[i];
+        }
+    }
+    return SPAI_OK;
+    API_END
+}
+
+int spai_get_column(spai_handle *h, int64_t k, int64_t *q, int64_t *pattern, double *coefficients) {
+    API_BEGIN
+    if (!h || !q || k < 0 || k >= h->n)
+        return fail(SPAI_ERR_ARGUMENT, "spai_get_column: bad arguments");
+    if (!h->built)
+        return fail(SPAI_ERR_NOT_BUILT, "no preconditioner built");
+    const bool f64 = h->precision == SPAI_PREC_F64;
+    int qs = 0;
+    long long off = -1;
+    const int *cq = f64 ? h->s64.col_q : h->s32.col_q;
+    const long long *co = f64 ? h->s64.packed_off : h->s32.packed_off;
+    if (!cq) {
+        *q = 0;
+        return SPAI_OK;
+    }
+    SPAI_CUDA(cudaMemcpy(&qs, cq + k, sizeof(int), cudaMemcpyDeviceToHost));
+    SPAI_CUDA(cudaMemcpy(&off, co + k, sizeof(long long), cudaMemcpyDeviceToHost));
+    *q = qs;
+    if (off < 0 || qs == 0)
+        return SPAI_OK;
+    std::vector<int> idx(qs);
+    SPAI_CUDA(cudaMemcpy(idx.data(), (f64 ? h->s64.packed_idx : h->s32.packed_idx) + off, sizeof(int) * qs, cudaMemcpyDeviceToHost));
+    if (pattern)
+        for (int i = 0; i < qs; ++i)
+            pattern[i] = idx[i];
+    if (coefficients) {
+        if (f64) {
+            SPAI_CUDA(cudaMemcpy(coefficients, h->s64.packed_val + off, sizeof(double) * qs, cudaMemcpyDeviceToHost));
+        } else {
+            std::vector<float> v(qs);
+            SPAI_CUDA(cudaMemcpy(v.data(), h->s32.packed_val + off, sizeof(float) * qs, cudaMemcpyDeviceToHost));
+            for (int i = 0; i < qs; ++i)
+                coefficients[i] = v[i];
+        }
+    }
+    return SPAI_OK;
+    API_END
+}
+
+int spai_spmv(spai_handle *h, int32_t which, const double *x, double *y) {
+    API_BEGIN
+    if (!h || !x || !y || which < 0 || which > 1)
+        return fail(SPAI_ERR_ARGUMENT, "spai_spmv: bad arguments");
+    if (which == 1 && !h->built)
+        return fail(SPAI_ERR_NOT_BUILT, "no preconditioner built");
+    SPAI_CUDA(cudaSetDevice(h->device));
+    const int n = h->n;
+    h->scratch.reset();
+    double *dx = h->scratch.alloc<double>(n);
+    double *dy = h->scratch.alloc<double>(n);
+    SPAI_CUDA(cudaMemcpyAsync(dx, x, sizeof(double) * n, cudaMemcpyHostToDevice, h->stream));
+    const VecRef<double> xr{dx, 0, nullptr, 0}, yr{dy, 0, nullptr, 0};
+    if (h->precision == SPAI_PREC_F64) {
+        launch_spmv<double, double, double>(which ? h->s64.p : h->a64, xr, yr, nullptr, h->sms, h->stream);
+    } else {
+        float *fx = h->scratch.alloc<float>(n);
+        float *fy = h->scratch.alloc<float>(n);
+        convert_kernel<float, double><<<grid_for(n, 256, h->sms * 8), 256, 0, h->stream>>>(n, dx, fx);
+        const VecRef<float> fxr{fx, 0, nullptr, 0}, fyr{fy, 0, nullptr, 0};
+        launch_spmv<float, float, float>(which ? h->s32.p : h->a32, fxr, fyr, nullptr, h->sms, h->stream);
+        convert_kernel<double, float><<<grid_for(n, 256, h->sms * 8), 256, 0, h->stream>>>(n, fy, dy);
+        SPAI_LAUNCH("convert_kernel");
+    }
+    SPAI_CUDA(cudaMemcpyAsync(y, dy, sizeof(double) * n, cudaMemcpyDeviceToHost, h->stream));
+    SPAI_CUDA(cudaStreamSynchronize(h->stream));
+    return SPAI_OK;
+    API_END
+}
+
+int spai_score(int32_t precision, double rsq, double dot, double den, double *out) {
+    API_BEGIN
+    if (!out)
+        return fail(SPAI_ERR_ARGUMENT, "spai_score: null output");
+    if (precision == SPAI_PREC_F64)
+        score_kat<double>(rsq, dot, den, out);
+    else
+        score_kat<float>(static_cast<float>(rsq), static_cast<float>(dot), static_cast<float>(den), out);
+    return SPAI_OK;
+    API_END
+}
+
+int spai_gmres(spai_handle *h, const double *rhs, double *x, double tau, int64_t cap,
+               int32_t *out_status, int64_t *out_iterations, double *out_relative) {
+    API_BEGIN
+    if (!h || !rhs || !x)
+        return fail(SPAI_ERR_ARGUMENT, "spai_gmres: null argument");
+    if (!h->built || h->spai_status != SPAI_SUCCESS)
+        return fail(SPAI_ERR_NOT_BUILT, "spai_gmres needs a successfully built preconditioner");
+    const int n = h->n;
+    if (cap < 0 || cap > n || !(tau > 0) || !std::isfinite(tau)) {
+        if (out_status)
+            *out_status = GMRES_INVALID_INPUT;
+        return SPAI_OK;
+    }
+    for (int i = 0; i < n; ++i)
+        if (!std::isfinite(rhs[i])) {
+            if (out_status)
+                *out_status = GMRES_INVALID_INPUT;
+            return SPAI_OK;
+        }
+    SPAI_CUDA(cudaSetDevice(h->device));
+    const int c = cap == 0 ? n : static_cast<int>(cap);
+    ensure_engine(h, c);
+    SolveSettings s;
+    s.cap = c;
+    s.tau = tau;
+    s.accept_every = h->precision == SPAI_PREC_F32;
+    h->scratch.reset();
+    double *dr = h->scratch.alloc<double>(n);
+    double *dx = h->scratch.alloc<double>(n);
+    SPAI_CUDA(cudaMemcpyAsync(dr, rhs, sizeof(double) * n, cudaMemcpyHostToDevice, h->stream));
+    Ctl ctl{};
+    auto run = [&](auto &e) {
+        using T = std::remove_pointer_t<decltype(e.rhs)>;
+        convert_kernel<T, double><<<grid_for(n, 256, h->sms * 8), 256, 0, h->stream>>>(n, dr, e.rhs);
+        SPAI_LAUNCH("convert_kernel");
+        e.gmres_only(h->stream, s, h->pinned);
+        read_ctl(h, e, ctl);
+        if (ctl.formed > 0) {
+            convert_kernel<double, T><<<grid_for(n, 256, h->sms * 8), 256, 0, h->stream>>>(n, e.cand, dx);
+            SPAI_LAUNCH("convert_kernel");
+        } else {
+            SPAI_CUDA(cudaMemsetAsync(dx, 0, sizeof(double) * n, h->stream));
+        }
+    };
+    if (h->precision == SPAI_PREC_F64)
+        run(h->e64);
+    else if (h->precision == SPAI_PREC_MIXED)
+        run(h->emix);
+    else
+        run(h->e32);
+    SPAI_CUDA(cudaMemcpyAsync(x, dx, sizeof(double) * n, cudaMemcpyDeviceToHost, h->stream));
+    SPAI_CUDA(cudaStreamSynchronize(h->stream));
+    if (out_status)
+        *out_status = ctl.status;
+    if (out_iterations)
+        *out_iterations = ctl.iterations;
+    if (out_relative)
+        *out_relative = ctl.rel;
+    return SPAI_OK;
+    API_END
+}
+
+int spai_ir_solve_batched(int64_t count, const spai_csr *systems, const double *const *b,
+                          double *const *x, const spai_options *opt, spai_report *reports,
+                          void *stream) {
+    (void)count;
+    (void)systems;
+    (void)b;
+    (void)x;
+    (void)opt;
+    (void)reports;
+    (void)stream;
+    return fail(SPAI_ERR_UNSUPPORTED, "spai_ir_solve_batched: not built yet");
+}
+
+int spai_adjoint(spai_handle *h, int64_t nrhs, const double *x, const double *dLdx, double *dLdb,
+                 double *dLdA_values, const spai_options *opt, spai_report *rep) {
+    (void)h;
+    (void)nrhs;
+    (void)x;
+    (void)dLdx;
+    (void)dLdb;
+    (void)dLdA_values;
+    (void)opt;
+    (void)rep;
+    return fail(SPAI_ERR_UNSUPPORTED, "spai_adjoint: not built yet");
+}
+
+} // extern "C"

@@ -1,0 +1,58 @@
+// Device-side GMRES / iterative-refinement state shared by krylov.cu and the API layer.
+#pragma once
+#include "spai_internal.hpp"
+
+namespace spai {
+
+// Control block in device memory. Every kernel of the Arnoldi step and the refinement loop
+// reads its loop state here, so the same launch sequence can be replayed by a CUDA graph.
+struct Ctl {
+    // GMRES
+    int k;           // current Arnoldi column
+    int cap;         // iteration cap
+    int active;      // GMRES loop still running
+    int status;      // GmresStatus of the current inner solve
+    int converged;
+    int triggered;   // candidate verification requested for column k
+    int breakdown;   // h(k+1,k) == 0
+    int iterations;
+    int formed;      // columns in the last formed candidate
+    int norm_rescale;
+    // IR
+    int outer_active;
+    int ir_status;
+    int outer_steps;
+    int inner_attempts;
+    int inner_iterations_total;
+    int changed;     // x + d != x somewhere (stagnation test)
+    int nonfinite;   // a refinement quantity overflowed
+    int last_gmres_status;
+    int ir_started;
+    int nrows;        // n: GMRES cap < n -> iteration_limit, else nonconvergence
+    int accept_every; // binary32 drop-in acceptance (verify every step)
+    int vgate;        // verification kernels of this step run
+    int pending;      // an update x_new = x + d awaits its diagnostics
+    int pad[1];
+    double be, cbe, rinf, xinf, bscale, anorm_inf, binf;
+    double inner_scale; // power of two applied to the correction right-hand side
+    double tol_inner;
+    double be_tol;
+    double den, beta, est, hnext, rel, orig;
+    int outer_cap;
+    int counters[16]; // last-block tickets
+};
+
+struct GmresBuffers; // defined in krylov.cu
+
+// Settings of one solve.
+struct SolveSettings {
+    int cap = 0;
+    int outer_cap = 20;
+    double tau = 1e-8;
+    double be_tol = 0;
+    bool scale_rhs = false; // mixed form: power-of-two scaled binary32 correction RHS
+    bool accept_every = false; // binary32 drop-in acceptance (recomputed residual each step)
+    bool use_graph = true;
+};
+
+} // namespace spai

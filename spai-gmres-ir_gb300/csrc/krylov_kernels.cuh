@@ -1,0 +1,1017 @@
+// GMRES (Arnoldi with classical Gram-Schmidt twice, Givens on the device) and the
+// iterative-refinement outer loop, all resident on the device.
+//
+// Reference path replaced:
+//   * CudaCsrSpmv / Matrix::apply (src/cuda_spmv.cu:177-203, src/cuda_gmres.cu:321-336):
+//     cuSPARSE CSR_ALG2 plus a memset and a finite-flag round trip per product.
+//   * Engine dot/axpy/norm (src/cuda_gmres.cu:238-280): one cuBLAS call and one host sync per
+//     modified Gram-Schmidt coefficient, a one-thread LASSQ norm kernel.
+//   * solve (src/cuda_gmres.cu:398-522): Givens, Hessenberg and the candidate solve on the host,
+//     a candidate formed and verified every iteration.
+//   * cuda_refine_with_preconditioner (src/cuda_ir.cpp:31-116): host residual, host update.
+// Here every step keeps its scalars on the device: the Hessenberg column, rotations and the
+// acceptance decision are computed by the last block of the final orthogonalisation pass, and the
+// candidate x0 + V y is formed and verified only when verification is triggered (estimate <= tau,
+// breakdown or the cap), which is the binary64 acceptance rule of src/gmres.cpp:238-241.
+// Orthogonalisation is CGS2 (two classical passes) instead of one modified pass: same Hessenberg
+// in exact arithmetic, O(1) grid synchronisations per step instead of O(k).
+// Reductions are deterministic: fixed grid, fixed per-thread row assignment, fixed tree order.
+#include "common.cuh"
+#include "exact_math.cuh"
+#pragma once
+#include "krylov.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+namespace spai {
+
+inline namespace kdetail {
+constexpr int kBlock = 256;
+
+template <class T> __device__ __forceinline__ T block_reduce_sum(T v, T *sh) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int o = 16; o > 0; o >>= 1)
+        v += __shfl_xor_sync(0xffffffffu, v, o);
+    __syncthreads();
+    if (lane == 0)
+        sh[w] = v;
+    __syncthreads();
+    T r = 0;
+    if (threadIdx.x < 32) {
+        r = threadIdx.x < (blockDim.x >> 5) ? sh[threadIdx.x] : T(0);
+        for (int o = 16; o > 0; o >>= 1)
+            r += __shfl_xor_sync(0xffffffffu, r, o);
+    }
+    return r; // valid in thread 0
+}
+template <class T> __device__ __forceinline__ T block_reduce_max(T v, T *sh) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int o = 16; o > 0; o >>= 1)
+        v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    __syncthreads();
+    if (lane == 0)
+        sh[w] = v;
+    __syncthreads();
+    T r = 0;
+    if (threadIdx.x < 32) {
+        r = threadIdx.x < (blockDim.x >> 5) ? sh[threadIdx.x] : T(0);
+        for (int o = 16; o > 0; o >>= 1)
+            r = fmax(r, __shfl_xor_sync(0xffffffffu, r, o));
+    }
+    return r;
+}
+
+// Last-block ticket: returns true in exactly one block, after every block has published.
+__device__ __forceinline__ bool last_block(int *counter) {
+    __shared__ int is_last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const int t = atomicAdd(counter, 1);
+        is_last = (t == static_cast<int>(gridDim.x) - 1);
+        if (is_last)
+            *counter = 0; // ready for the next launch
+    }
+    __syncthreads();
+    if (is_last)
+        __threadfence();
+    return is_last != 0;
+}
+
+// Overflow-safe 2-norm partial: (exponent, scaled sum of squares) with a power-of-two scale.
+struct NormPart {
+    int e;
+    double s;
+};
+template <class T> __device__ __forceinline__ int exp_of(T m) {
+    return m > T(0) ? ilogb(m) : INT_MIN;
+}
+
+// Resolve a vector that lives at base + index*stride where index is read on the device.
+template <class T> struct VecRef {
+    T *base;
+    long long stride;
+    const int *index; // nullptr: offset 0
+    int add;          // added to *index
+    __device__ __forceinline__ T *get() const {
+        return index ? base + static_cast<long long>(*index + add) * stride : base;
+    }
+};
+
+enum Slot : int {
+    kSlotDots = 0,
+    kSlotUpdNorm,
+    kSlotNormA,
+    kSlotNormB,
+    kSlotDiag,
+    kSlotCand,
+    kSlotMisc
+};
+
+// ------------------------------------------------------------------------------------------
+// SpMV: G lanes per row, row-per-group grid stride; accumulate in the output type.
+// ------------------------------------------------------------------------------------------
+template <class TA, class TX, class TY, int G>
+__global__ void __launch_bounds__(kBlock) spmv_kernel(int n, const int *__restrict__ rp,
+                                                      const int *__restrict__ ci,
+                                                      const TA *__restrict__ av, VecRef<TX> xr,
+                                                      VecRef<TY> yr, const int *gate) {
+    if (gate && !*gate)
+        return;
+    const TX *__restrict__ x = xr.get();
+    TY *__restrict__ y = yr.get();
+    const int lane = threadIdx.x & (G - 1);
+    const int groups = (gridDim.x * blockDim.x) / G;
+    // Warp-uniform loop: every lane of a warp runs the same trip count, so the group shuffles
+    // always see all 32 lanes.
+    const int warp_first = (blockIdx.x * blockDim.x + (threadIdx.x & ~31)) / G;
+    const int sub = (threadIdx.x & 31) / G;
+    for (int base = warp_first; base < n; base += groups) {
+        const int row = base + sub;
+        TY acc = 0;
+        if (row < n) {
+            const int b = rp[row], e = rp[row + 1];
+            for (int t = b + lane; t < e; t += G)
+                acc += static_cast<TY>(av[t]) * static_cast<TY>(__ldg(&x[ci[t]]));
+        }
+        for (int o = G / 2; o > 0; o >>= 1)
+            acc += __shfl_xor_sync(0xffffffffu, acc, o, G);
+        if (lane == 0 && row < n)
+            y[row] = acc;
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// Norm of a vector (or of a - b) with a last-block finish; result written to *out.
+// ------------------------------------------------------------------------------------------
+template <class T>
+__global__ void __launch_bounds__(kBlock) norm_kernel(int n, VecRef<T> ar, const T *bsub,
+                                                      NormPart *part, int *counter, T *out,
+                                                      const int *gate) {
+    if (gate && !*gate)
+        return;
+    __shared__ T sh[32];
+    __shared__ double shd[32];
+    const T *a = ar.get();
+    const int stride = gridDim.x * blockDim.x;
+    T mx = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const T v = bsub ? a[i] - bsub[i] : a[i];
+        mx = fmax(mx, fabs(v));
+    }
+    const T bmax = block_reduce_max(mx, sh);
+    __shared__ int be;
+    if (threadIdx.x == 0)
+        be = exp_of(bmax);
+    __syncthreads();
+    double s = 0;
+    if (be != INT_MIN) {
+        const T scale = ldexp(T(1), -be);
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+            const T v = (bsub ? a[i] - bsub[i] : a[i]) * scale;
+            s += static_cast<double>(v) * static_cast<double>(v);
+        }
+    }
+    // The per-element scaled square is accumulated in binary64 only here, in a reduction over
+    // at most a few thousand elements per thread pair of sweeps; the vector work stays in T.
+    const double bs = block_reduce_sum(s, shd);
+    if (threadIdx.x == 0)
+        part[blockIdx.x] = NormPart{be, bs};
+    if (!last_block(counter))
+        return;
+    if (threadIdx.x == 0) {
+        int E = INT_MIN;
+        bool nonfinite = false;
+        for (int b = 0; b < static_cast<int>(gridDim.x); ++b) {
+            E = max(E, part[b].e);
+            nonfinite |= !isfinite(part[b].s);
+        }
+        double S = 0;
+        if (E != INT_MIN)
+            for (int b = 0; b < static_cast<int>(gridDim.x); ++b)
+                if (part[b].e != INT_MIN)
+                    S += ldexp(part[b].s, 2 * (part[b].e - E));
+        T r = E == INT_MIN ? T(0) : static_cast<T>(ldexp(sqrt(S), E));
+        if (nonfinite)
+            r = T(INFINITY);
+        *out = r;
+    }
+}
+} // namespace kdetail
+
+// ------------------------------------------------------------------------------------------
+// Arnoldi passes.
+// ------------------------------------------------------------------------------------------
+// dots: part[b*ps + j] = sum over the block's rows of V_j[i] * w[i], j = 0..k. Last block
+// reduces into h[j]. Grid-stride over row tiles, one warp per basis vector within a tile.
+template <class T, int TILE>
+__global__ void __launch_bounds__(kBlock) arnoldi_dots_kernel(int n, long long ld, const T *V,
+                                                              const T *w, const Ctl *ctl, T *part,
+                                                              int ps, T *h, int *counter) {
+    if (!ctl->active)
+        return;
+    extern __shared__ __align__(16) unsigned char dyn[];
+    T *acc = reinterpret_cast<T *>(dyn); // [k+1]
+    __shared__ T wt[TILE];
+    const int k = ctl->k;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int j = threadIdx.x; j <= k; j += blockDim.x)
+        acc[j] = 0;
+    for (long long r0 = static_cast<long long>(blockIdx.x) * TILE; r0 < n;
+         r0 += static_cast<long long>(gridDim.x) * TILE) {
+        const int rows = static_cast<int>(min(static_cast<long long>(TILE), n - r0));
+        __syncthreads();
+        for (int i = threadIdx.x; i < TILE; i += blockDim.x)
+            wt[i] = i < rows ? w[r0 + i] : T(0);
+        __syncthreads();
+        for (int j = warp; j <= k; j += nw) {
+            const T *vj = V + static_cast<long long>(j) * ld + r0;
+            T s = 0;
+#pragma unroll 4
+            for (int i = lane; i < rows; i += 32)
+                s += vj[i] * wt[i];
+            for (int o = 16; o > 0; o >>= 1)
+                s += __shfl_xor_sync(0xffffffffu, s, o);
+            if (lane == 0)
+                acc[j] += s;
+        }
+    }
+    __syncthreads();
+    for (int j = threadIdx.x; j <= k; j += blockDim.x)
+        part[static_cast<long long>(blockIdx.x) * ps + j] = acc[j];
+    if (!last_block(counter))
+        return;
+    for (int j = threadIdx.x; j <= k; j += blockDim.x) {
+        T s = 0;
+        for (int b = 0; b < static_cast<int>(gridDim.x); ++b)
+            s += part[static_cast<long long>(b) * ps + j];
+        h[j] = s;
+    }
+}
+
+// update: w[i] -= sum_j V_j[i] h[j]; optionally accumulate the norm partial of the new w and,
+// in the last block, finish the Arnoldi column: H(:,k) = h1 + h2, h(k+1,k) = ||w||, Givens.
+template <class T>
+__global__ void __launch_bounds__(kBlock) arnoldi_update_kernel(int n, long long ld, const T *V,
+                                                                T *w, Ctl *ctl, const T *h,
+                                                                NormPart *npart, int *counter,
+                                                                int finish, const T *h1, T *H,
+                                                                int hld, T *cs, T *sn, T *g) {
+    if (!ctl->active)
+        return;
+    __shared__ T sh[32];
+    __shared__ double shd[32];
+    __shared__ int be;
+    const int k = ctl->k;
+    const int stride = gridDim.x * blockDim.x;
+    T mx = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        T acc = w[i];
+#pragma unroll 8
+        for (int j = 0; j <= k; ++j)
+            acc -= V[static_cast<long long>(j) * ld + i] * h[j];
+        w[i] = acc;
+        mx = fmax(mx, fabs(acc));
+    }
+    if (!finish)
+        return;
+    const T bmax = block_reduce_max(mx, sh);
+    if (threadIdx.x == 0)
+        be = exp_of(bmax);
+    __syncthreads();
+    double s = 0;
+    if (be != INT_MIN) {
+        const T scale = ldexp(T(1), -be);
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+            const T v = w[i] * scale;
+            s += static_cast<double>(v) * static_cast<double>(v);
+        }
+    }
+    const double bs = block_reduce_sum(s, shd);
+    if (threadIdx.x == 0)
+        npart[blockIdx.x] = NormPart{be, bs};
+    if (!last_block(counter))
+        return;
+    if (threadIdx.x != 0)
+        return;
+    // ---- Arnoldi column k and Givens update (src/gmres.cpp:174-214) ----
+    int E = INT_MIN;
+    bool nonfinite = !isfinite(static_cast<double>(bmax));
+    for (int b = 0; b < static_cast<int>(gridDim.x); ++b) {
+        E = max(E, npart[b].e);
+        nonfinite |= !isfinite(npart[b].s);
+    }
+    double S = 0;
+    if (E != INT_MIN)
+        for (int b = 0; b < static_cast<int>(gridDim.x); ++b)
+            if (npart[b].e != INT_MIN)
+                S += ldexp(npart[b].s, 2 * (npart[b].e - E));
+    const T hnext = E == INT_MIN ? T(0) : static_cast<T>(ldexp(sqrt(S), E));
+    T *col = H + static_cast<long long>(k) * hld;
+    for (int j = 0; j <= k; ++j) {
+        col[j] = h1[j] + h[j];
+        nonfinite |= !isfinite(col[j]);
+    }
+    col[k + 1] = hnext;
+    nonfinite |= !isfinite(hnext);
+    ctl->hnext = static_cast<double>(hnext);
+    ctl->breakdown = hnext == T(0);
+    for (int r = 0; r < k; ++r) {
+        const T up = col[r], lo = col[r + 1];
+        col[r] = cs[r] * up + sn[r] * lo;
+        col[r + 1] = -sn[r] * up + cs[r] * lo;
+    }
+    const T upper = col[k];
+    const T radius = cr_hypot<T>(upper, col[k + 1]);
+    ctl->iterations = k + 1;
+    if (nonfinite || !isfinite(radius)) {
+        ctl->status = 8; // numerical_failure
+        ctl->active = 0;
+        ctl->triggered = 0;
+        ctl->vgate = 0;
+        return;
+    }
+    if (radius == T(0)) {
+        // Zero Givens pivot: verify the previously defined candidate (gmres.cpp:218-234).
+        ctl->triggered = 2;
+        ctl->vgate = 1;
+        return;
+    }
+    cs[k] = upper / radius;
+    sn[k] = col[k + 1] / radius;
+    col[k] = radius;
+    col[k + 1] = 0;
+    const T old = g[k];
+    g[k] = cs[k] * old;
+    g[k + 1] = -sn[k] * old;
+    const T est = fabs(g[k + 1]) / static_cast<T>(ctl->den);
+    ctl->est = static_cast<double>(est);
+    const bool trig = ctl->breakdown || est <= static_cast<T>(ctl->tol_inner) || k + 1 == ctl->cap;
+    ctl->triggered = trig ? 1 : 0;
+    ctl->vgate = (trig || ctl->accept_every) ? 1 : 0;
+}
+
+// v_{k+1} = w / h(k+1,k) (skipped on breakdown).
+template <class T>
+__global__ void __launch_bounds__(kBlock) normalize_kernel(int n, long long ld, T *V, const T *w,
+                                                           const Ctl *ctl) {
+    if (!ctl->active || ctl->breakdown || ctl->triggered == 2 || ctl->status == 8)
+        return;
+    const T h = static_cast<T>(ctl->hnext);
+    T *v = V + static_cast<long long>(ctl->k + 1) * ld;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        v[i] = w[i] / h;
+}
+
+// Back substitution y = R^{-1} g over `count` columns (src/gmres.cpp:47-55); count = k+1, or k
+// when the zero-pivot branch re-verifies the previous candidate. One block.
+template <class T>
+__global__ void solve_y_kernel(Ctl *ctl, const T *H, int hld, const T *g, T *y) {
+    if (!ctl->active || !ctl->vgate)
+        return;
+    const int k = ctl->k;
+    const int count = ctl->triggered == 2 ? k : k + 1;
+    if (threadIdx.x == 0) {
+        bool bad = false;
+        for (int r = count - 1; r >= 0; --r) {
+            T v = g[r];
+            for (int c = r + 1; c < count; ++c)
+                v -= H[static_cast<long long>(c) * hld + r] * y[c];
+            y[r] = v / H[static_cast<long long>(r) * hld + r];
+            bad |= !isfinite(y[r]);
+        }
+        ctl->formed = count;
+        if (bad) {
+            ctl->status = 8;
+            ctl->active = 0;
+        }
+    }
+}
+
+// x = sum_j y_j V_j over the formed columns (x0 = 0 in every correction solve).
+template <class T>
+__global__ void __launch_bounds__(kBlock) form_candidate_kernel(int n, long long ld, const T *V,
+                                                                const T *y, T *x, const Ctl *ctl) {
+    if (!ctl->active || !ctl->vgate)
+        return;
+    const int count = ctl->formed;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        T acc = 0;
+#pragma unroll 8
+        for (int j = 0; j < count; ++j)
+            acc += V[static_cast<long long>(j) * ld + i] * y[j];
+        x[i] = acc;
+    }
+}
+
+// Acceptance (src/gmres.cpp:235-253): accepted iff verification triggered and the recomputed
+// preconditioned residual <= tau; breakdown ends the solve either way; otherwise advance k.
+template <class T>
+__global__ void decide_kernel(Ctl *ctl, const T *orig, const T *relnum) {
+    if (threadIdx.x != 0 || !ctl->active)
+        return;
+    const int accept_every = ctl->accept_every;
+    const bool verified = ctl->vgate != 0;
+    ctl->vgate = 0;
+    if (verified) {
+        const double rel = static_cast<double>(*relnum) / ctl->den;
+        ctl->rel = rel;
+        ctl->orig = static_cast<double>(*orig);
+        if (!isfinite(rel) || !isfinite(ctl->orig)) {
+            ctl->status = 8;
+            ctl->active = 0;
+            return;
+        }
+        const bool ok = rel <= ctl->tol_inner;
+        if (ctl->triggered == 2) { // zero Givens pivot
+            ctl->converged = ok && !accept_every;
+            ctl->status = ctl->converged ? 0 : 5;
+            ctl->active = 0;
+            return;
+        }
+        if (ok) {
+            ctl->converged = 1;
+            ctl->status = 0;
+            ctl->active = 0;
+            return;
+        }
+        if (ctl->breakdown) {
+            ctl->status = 5;
+            ctl->active = 0;
+            return;
+        }
+    }
+    if (ctl->k + 1 >= ctl->cap) {
+        ctl->status = ctl->cap < ctl->nrows ? 6 : 7; // iteration_limit / nonconvergence
+        ctl->active = 0;
+        return;
+    }
+    ctl->k += 1;
+    ctl->triggered = 0;
+}
+
+// ------------------------------------------------------------------------------------------
+// GMRES start: r0 = rhs (x0 = 0). Zero RHS -> converged with d = 0. Then Pb, its norm and v0.
+// ------------------------------------------------------------------------------------------
+template <class T> __global__ void gmres_start_kernel(Ctl *ctl, const T *orig, int accept_every) {
+    if (threadIdx.x != 0 || !ctl->outer_active)
+        return;
+    ctl->k = 0;
+    ctl->triggered = 0;
+    ctl->breakdown = 0;
+    ctl->converged = 0;
+    ctl->iterations = 0;
+    ctl->formed = 0;
+    ctl->active = 1;
+    ctl->status = 7;
+    const double r0 = static_cast<double>(*orig);
+    ctl->orig = r0;
+    if (!isfinite(r0)) {
+        ctl->status = 8;
+        ctl->active = 0;
+        return;
+    }
+    if (r0 == 0) {
+        ctl->status = accept_every ? 2 : 1; // exact_initial_solution (binary32) / zero_rhs
+        ctl->converged = 1;
+        ctl->active = 0;
+        ctl->formed = -1; // correction is exactly zero
+    }
+}
+template <class T>
+__global__ void gmres_den_kernel(Ctl *ctl, const T *den, T *g, int accept_every) {
+    if (threadIdx.x != 0 || !ctl->active)
+        return;
+    const double d = static_cast<double>(*den);
+    ctl->den = d;
+    if (!isfinite(d)) {
+        ctl->status = 8;
+        ctl->active = 0;
+        return;
+    }
+    if (d == 0) {
+        ctl->status = 4; // zero_preconditioned_rhs
+        ctl->active = 0;
+        return;
+    }
+    ctl->beta = d;
+    if (1.0 <= ctl->tol_inner) { // initial relative residual beta/den = 1
+        ctl->status = 0;
+        ctl->converged = 1;
+        ctl->active = 0;
+        ctl->formed = -1;
+        return;
+    }
+    g[0] = static_cast<T>(d);
+}
+template <class T>
+__global__ void __launch_bounds__(kBlock) scale_into_kernel(int n, const T *src, T *dst,
+                                                            const Ctl *ctl) {
+    if (!ctl->active)
+        return;
+    const T d = static_cast<T>(ctl->den);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        dst[i] = src[i] / d;
+}
+
+// ------------------------------------------------------------------------------------------
+// Iterative refinement in TO (binary64 for F64/MIXED, binary32 for F32).
+// ------------------------------------------------------------------------------------------
+struct DiagPart {
+    double rinf, xinf, cbe;
+    int nonfinite;
+};
+
+// r = b - A x with the normwise and componentwise backward errors (src/ir.cpp:83-133).
+template <class TO, int G>
+__global__ void __launch_bounds__(kBlock) ir_residual_kernel(int n, const int *__restrict__ rp,
+                                                             const int *__restrict__ ci,
+                                                             const TO *__restrict__ av,
+                                                             const TO *__restrict__ x,
+                                                             const TO *__restrict__ b, TO *r,
+                                                             DiagPart *part, Ctl *ctl,
+                                                             int *counter) {
+    if (!ctl->outer_active)
+        return;
+    __shared__ double sh[32];
+    const int lane = threadIdx.x & (G - 1);
+    const int groups = (gridDim.x * blockDim.x) / G;
+    double rinf = 0, xinf = 0, cbe = 0;
+    int bad = 0;
+    const int warp_first = (blockIdx.x * blockDim.x + (threadIdx.x & ~31)) / G;
+    const int sub = (threadIdx.x & 31) / G;
+    for (int base = warp_first; base < n; base += groups) {
+        const int row = base + sub;
+        TO acc = 0, absacc = 0;
+        if (row < n) {
+            const int s = rp[row], e = rp[row + 1];
+            for (int t = s + lane; t < e; t += G) {
+                const TO xv = x[ci[t]];
+                acc += av[t] * xv;
+                absacc += fabs(av[t]) * fabs(xv);
+            }
+        }
+        for (int o = G / 2; o > 0; o >>= 1) {
+            acc += __shfl_xor_sync(0xffffffffu, acc, o, G);
+            absacc += __shfl_xor_sync(0xffffffffu, absacc, o, G);
+        }
+        if (lane == 0 && row < n) {
+            const TO res = b[row] - acc;
+            r[row] = res;
+            bad |= !isfinite(res) || !isfinite(absacc);
+            rinf = fmax(rinf, static_cast<double>(fabs(res)));
+            xinf = fmax(xinf, static_cast<double>(fabs(x[row])));
+            const double cden = static_cast<double>(fabs(b[row]) + absacc);
+            const double ratio = cden == 0 ? (res == TO(0) ? 0.0 : INFINITY)
+                                           : static_cast<double>(fabs(res)) / cden;
+            cbe = fmax(cbe, ratio);
+        }
+    }
+    rinf = block_reduce_max(rinf, sh);
+    __syncthreads();
+    xinf = block_reduce_max(xinf, sh);
+    __syncthreads();
+    cbe = block_reduce_max(cbe, sh);
+    bad = __syncthreads_or(bad);
+    if (threadIdx.x == 0)
+        part[blockIdx.x] = DiagPart{rinf, xinf, cbe, bad};
+    if (!last_block(counter))
+        return;
+    if (threadIdx.x != 0)
+        return;
+    double R = 0, X = 0, C = 0;
+    int nonfinite = 0;
+    for (int i = 0; i < static_cast<int>(gridDim.x); ++i) {
+        R = fmax(R, part[i].rinf);
+        X = fmax(X, part[i].xinf);
+        C = fmax(C, part[i].cbe);
+        nonfinite |= part[i].nonfinite;
+    }
+    ctl->rinf = R;
+    ctl->xinf = X;
+    ctl->cbe = C;
+    const TO den = static_cast<TO>(ctl->anorm_inf) * static_cast<TO>(X) + static_cast<TO>(ctl->binf);
+    if (nonfinite || !isfinite(den)) {
+        ctl->ir_status = 6; // numerical_failure
+        ctl->outer_active = 0;
+        return;
+    }
+    const double be = den == TO(0) ? (R == 0 ? 0.0 : INFINITY) : static_cast<double>(static_cast<TO>(R) / den);
+    ctl->be = be;
+    if (be <= ctl->be_tol) {
+        ctl->ir_status = 0;
+        ctl->outer_active = 0;
+        return;
+    }
+    if (ctl->ir_started && !ctl->changed) {
+        ctl->ir_status = 4; // stagnation
+        ctl->outer_active = 0;
+        return;
+    }
+    if (ctl->outer_steps >= ctl->outer_cap) {
+        ctl->ir_status = 5; // iteration_limit
+        ctl->outer_active = 0;
+        return;
+    }
+    // Power-of-two scale for the correction right-hand side (mixed form), exact in binary64.
+    ctl->inner_scale = ctl->bscale > 0 ? ldexp(1.0, -ilogb(R)) : 1.0;
+    ctl->ir_started = 1;
+    ctl->changed = 0;
+}
+
+template <class TO, class T>
+__global__ void __launch_bounds__(kBlock) make_rhs_kernel(int n, const TO *r, T *rhs, const Ctl *ctl) {
+    if (!ctl->outer_active)
+        return;
+    const TO s = static_cast<TO>(ctl->inner_scale);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        rhs[i] = static_cast<T>(r[i] * s);
+}
+
+// x += d (d = correction / scale); records whether any component changed.
+template <class TO, class T>
+__global__ void __launch_bounds__(kBlock) ir_update_kernel(int n, const TO *x, TO *xn, const T *d,
+                                                           Ctl *ctl) {
+    if (!ctl->outer_active)
+        return;
+    __shared__ int any;
+    if (threadIdx.x == 0)
+        any = 0;
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+        ctl->pending = 1;
+    __syncthreads();
+    const bool zero = ctl->formed < 0;
+    const TO inv = static_cast<TO>(1.0 / ctl->inner_scale); // exact: power of two
+    int changed = 0, bad = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const TO old = x[i];
+        const TO nw = zero ? old : old + static_cast<TO>(d[i]) * inv;
+        xn[i] = nw;
+        changed |= nw != old;
+        bad |= !isfinite(nw);
+    }
+    if (changed)
+        any = 1;
+    if (bad)
+        atomicOr(&ctl->nonfinite, 1);
+    __syncthreads();
+    if (threadIdx.x == 0 && any)
+        atomicOr(&ctl->changed, 1);
+}
+
+// Commit x <- x_new unless the new iterate's diagnostics failed (src/ir.cpp:176-186: a
+// converged correction is not committed after failed outer diagnostics).
+template <class TO>
+__global__ void __launch_bounds__(kBlock) ir_commit_kernel(int n, TO *x, const TO *xn, const Ctl *ctl) {
+    if (!ctl->pending || ctl->ir_status == 6)
+        return;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        x[i] = xn[i];
+}
+
+// After an inner solve: failure ends the loop with inner_failure; otherwise count the step.
+__global__ void ir_after_inner_kernel(Ctl *ctl) {
+    if (threadIdx.x != 0)
+        return;
+    ctl->pending = 0;
+    if (!ctl->outer_active)
+        return;
+    ctl->inner_attempts += 1;
+    ctl->inner_iterations_total += ctl->iterations;
+    ctl->last_gmres_status = ctl->status;
+    if (!ctl->converged) {
+        ctl->ir_status = 3; // inner_failure
+        ctl->outer_active = 0;
+    }
+}
+__global__ void ir_after_update_kernel(Ctl *ctl) {
+    if (threadIdx.x != 0 || !ctl->outer_active)
+        return;
+    if (ctl->nonfinite) {
+        ctl->ir_status = 6;
+        ctl->outer_active = 0;
+        return;
+    }
+    ctl->outer_steps += 1;
+}
+
+// x0 = P b with P in T and b, x in TO.
+template <class T, class TO>
+__global__ void __launch_bounds__(kBlock) ir_x0_kernel(int n, const int *__restrict__ rp,
+                                                       const int *__restrict__ ci,
+                                                       const T *__restrict__ pv,
+                                                       const TO *__restrict__ b, TO *x) {
+    for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < n; row += gridDim.x * blockDim.x) {
+        TO acc = 0;
+        for (int t = rp[row]; t < rp[row + 1]; ++t)
+            acc += static_cast<TO>(pv[t]) * b[ci[t]];
+        x[row] = acc;
+    }
+}
+
+// ||A||_inf and ||b||_inf (constant over the solve).
+template <class TO>
+__global__ void __launch_bounds__(kBlock) norms_inf_kernel(int n, const int *__restrict__ rp,
+                                                           const TO *__restrict__ av,
+                                                           const TO *__restrict__ b,
+                                                           DiagPart *part, Ctl *ctl, int *counter) {
+    __shared__ double sh[32];
+    double an = 0, bn = 0;
+    for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < n; row += gridDim.x * blockDim.x) {
+        TO s = 0;
+        for (int t = rp[row]; t < rp[row + 1]; ++t)
+            s += fabs(av[t]);
+        an = fmax(an, static_cast<double>(s));
+        bn = fmax(bn, static_cast<double>(fabs(b[row])));
+    }
+    an = block_reduce_max(an, sh);
+    __syncthreads();
+    bn = block_reduce_max(bn, sh);
+    if (threadIdx.x == 0)
+        part[blockIdx.x] = DiagPart{an, bn, 0, 0};
+    if (!last_block(counter))
+        return;
+    if (threadIdx.x == 0) {
+        double A = 0, B = 0;
+        for (int i = 0; i < static_cast<int>(gridDim.x); ++i) {
+            A = fmax(A, part[i].rinf);
+            B = fmax(B, part[i].xinf);
+        }
+        ctl->anorm_inf = A;
+        ctl->binf = B;
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// Host orchestration.
+// ------------------------------------------------------------------------------------------
+template <class T> int pick_group(const DeviceCsr<T> &m) {
+    const double avg = m.n ? static_cast<double>(m.nnz) / m.n : 1.0;
+    if (avg <= 2.5)
+        return 2;
+    if (avg <= 6)
+        return 4;
+    if (avg <= 12)
+        return 8;
+    if (avg <= 24)
+        return 16;
+    return 32;
+}
+
+template <class TA, class TX, class TY>
+void launch_spmv(const DeviceCsr<TA> &m, VecRef<TX> x, VecRef<TY> y, const int *gate, int sms,
+                 cudaStream_t st) {
+    const int G = pick_group(m);
+    const long long threads = static_cast<long long>(m.n) * G;
+    const unsigned blocks = grid_for(threads, kBlock, sms * 16);
+    switch (G) {
+    case 2:
+        spmv_kernel<TA, TX, TY, 2><<<blocks, kBlock, 0, st>>>(m.n, m.rp, m.ci, m.val, x, y, gate);
+        break;
+    case 4:
+        spmv_kernel<TA, TX, TY, 4><<<blocks, kBlock, 0, st>>>(m.n, m.rp, m.ci, m.val, x, y, gate);
+        break;
+    case 8:
+        spmv_kernel<TA, TX, TY, 8><<<blocks, kBlock, 0, st>>>(m.n, m.rp, m.ci, m.val, x, y, gate);
+        break;
+    case 16:
+        spmv_kernel<TA, TX, TY, 16><<<blocks, kBlock, 0, st>>>(m.n, m.rp, m.ci, m.val, x, y, gate);
+        break;
+    default:
+        spmv_kernel<TA, TX, TY, 32><<<blocks, kBlock, 0, st>>>(m.n, m.rp, m.ci, m.val, x, y, gate);
+    }
+    SPAI_LAUNCH("spmv_kernel");
+}
+
+// Buffers and launch sequence of one refinement solve with inner type T and outer type TO.
+template <class T, class TO> struct IrEngine {
+    int n = 0, cap = 0, sms = 0;
+    long long ld = 0;
+    int hld = 0;
+    const DeviceCsr<TO> *a_outer = nullptr;
+    const DeviceCsr<T> *a_inner = nullptr;
+    const DeviceCsr<T> *p = nullptr;
+    Ctl *ctl = nullptr;
+    T *V = nullptr, *w = nullptr, *t = nullptr, *rhs = nullptr, *pb = nullptr, *cand = nullptr,
+      *ax = nullptr, *pax = nullptr, *H = nullptr, *cs = nullptr, *sn = nullptr, *g = nullptr,
+      *y = nullptr, *h1 = nullptr, *h2 = nullptr, *part = nullptr, *scal = nullptr;
+    TO *r = nullptr, *xn = nullptr;
+    NormPart *npart = nullptr;
+    DiagPart *dpart = nullptr;
+    int *counters = nullptr;
+    int nblk_vec = 0, nblk_dots = 0;
+    long long launches = 0;
+
+    void setup(DeviceArena &arena, const DeviceCsr<TO> &ao, const DeviceCsr<T> &ai,
+               const DeviceCsr<T> &pp, int cap_, int sms_) {
+        a_outer = &ao;
+        a_inner = &ai;
+        p = &pp;
+        n = ai.n;
+        cap = cap_;
+        sms = sms_;
+        ld = (static_cast<long long>(n) + 31) & ~31LL;
+        hld = cap + 2;
+        nblk_vec = static_cast<int>(grid_for(n, kBlock, sms * 8));
+        nblk_dots = static_cast<int>(grid_for((n + 127) / 128, 1, sms * 4));
+        ctl = arena.alloc<Ctl>(1);
+        V = arena.alloc<T>(static_cast<size_t>(ld) * (cap + 1));
+        w = arena.alloc<T>(ld);
+        t = arena.alloc<T>(ld);
+        rhs = arena.alloc<T>(ld);
+        pb = arena.alloc<T>(ld);
+        cand = arena.alloc<T>(ld);
+        ax = arena.alloc<T>(ld);
+        pax = arena.alloc<T>(ld);
+        r = arena.alloc<TO>(ld);
+        xn = arena.alloc<TO>(ld);
+        H = arena.alloc<T>(static_cast<size_t>(hld) * (cap + 1));
+        cs = arena.alloc<T>(cap + 1);
+        sn = arena.alloc<T>(cap + 1);
+        g = arena.alloc<T>(cap + 2);
+        y = arena.alloc<T>(cap + 1);
+        h1 = arena.alloc<T>(cap + 2);
+        h2 = arena.alloc<T>(cap + 2);
+        part = arena.alloc<T>(static_cast<size_t>(std::max(nblk_dots, nblk_vec)) * (cap + 2));
+        npart = arena.alloc<NormPart>(std::max(nblk_dots, nblk_vec));
+        dpart = arena.alloc<DiagPart>(std::max(nblk_dots, nblk_vec));
+        scal = arena.alloc<T>(8);
+        counters = arena.alloc<int>(16);
+    }
+
+    VecRef<T> fixed(T *p_) const {
+        return VecRef<T>{p_, 0, nullptr, 0};
+    }
+    VecRef<T> basis_at_k(int add) const {
+        return VecRef<T>{V, ld, &ctl->k, add};
+    }
+
+    void norm(cudaStream_t st, VecRef<T> a, const T *bsub, T *out, int slot, const int *gate) {
+        norm_kernel<T><<<nblk_vec, kBlock, 0, st>>>(n, a, bsub, npart, counters + slot, out, gate);
+        SPAI_LAUNCH("norm_kernel");
+        ++launches;
+    }
+
+    // One Arnoldi step plus (when triggered) candidate verification.
+    void arnoldi_step(cudaStream_t st) {
+        launch_spmv<T, T, T>(*a_inner, basis_at_k(0), fixed(t), &ctl->active, sms, st);
+        launch_spmv<T, T, T>(*p, fixed(t), fixed(w), &ctl->active, sms, st);
+        const size_t dyn = sizeof(T) * static_cast<size_t>(cap + 2);
+        arnoldi_dots_kernel<T, 128><<<nblk_dots, kBlock, dyn, st>>>(n, ld, V, w, ctl, part, cap + 2,
+                                                                     h1, counters + kSlotDots);
+        SPAI_LAUNCH("arnoldi_dots_kernel");
+        arnoldi_update_kernel<T><<<nblk_vec, kBlock, 0, st>>>(n, ld, V, w, ctl, h1, npart,
+                                                               counters + kSlotUpdNorm, 0, nullptr,
+                                                               H, hld, cs, sn, g);
+        SPAI_LAUNCH("arnoldi_update_kernel(1)");
+        arnoldi_dots_kernel<T, 128><<<nblk_dots, kBlock, dyn, st>>>(n, ld, V, w, ctl, part, cap + 2,
+                                                                     h2, counters + kSlotDots);
+        SPAI_LAUNCH("arnoldi_dots_kernel(2)");
+        arnoldi_update_kernel<T><<<nblk_vec, kBlock, 0, st>>>(n, ld, V, w, ctl, h2, npart,
+                                                               counters + kSlotUpdNorm, 1, h1, H,
+                                                               hld, cs, sn, g);
+        SPAI_LAUNCH("arnoldi_update_kernel(2)");
+        normalize_kernel<T><<<nblk_vec, kBlock, 0, st>>>(n, ld, V, w, ctl);
+        SPAI_LAUNCH("normalize_kernel");
+        launches += 7;
+        verify(st);
+    }
+
+    void verify(cudaStream_t st) {
+        solve_y_kernel<T><<<1, 32, 0, st>>>(ctl, H, hld, g, y);
+        SPAI_LAUNCH("solve_y_kernel");
+        form_candidate_kernel<T><<<nblk_vec, kBlock, 0, st>>>(n, ld, V, y, cand, ctl);
+        SPAI_LAUNCH("form_candidate_kernel");
+        const int *g2 = &ctl->vgate;
+        launch_spmv<T, T, T>(*a_inner, fixed(cand), fixed(ax), g2, sms, st);
+        norm(st, fixed(rhs), ax, scal + 0, kSlotNormA, g2);
+        launch_spmv<T, T, T>(*p, fixed(ax), fixed(pax), g2, sms, st);
+        norm(st, fixed(pb), pax, scal + 1, kSlotNormB, g2);
+        decide_kernel<T><<<1, 32, 0, st>>>(ctl, scal + 0, scal + 1);
+        SPAI_LAUNCH("decide_kernel");
+        launches += 5;
+    }
+
+    // GMRES start for the current rhs (x0 = 0): ||rhs||, Pb, ||Pb||, v0 = Pb/||Pb||.
+    void gmres_start(cudaStream_t st, bool accept_every) {
+        norm(st, fixed(rhs), nullptr, scal + 2, kSlotNormA, &ctl->outer_active);
+        gmres_start_kernel<T><<<1, 32, 0, st>>>(ctl, scal + 2, accept_every ? 1 : 0);
+        SPAI_LAUNCH("gmres_start_kernel");
+        launch_spmv<T, T, T>(*p, fixed(rhs), fixed(pb), &ctl->active, sms, st);
+        norm(st, fixed(pb), nullptr, scal + 3, kSlotNormB, &ctl->active);
+        gmres_den_kernel<T><<<1, 32, 0, st>>>(ctl, scal + 3, g, accept_every ? 1 : 0);
+        SPAI_LAUNCH("gmres_den_kernel");
+        scale_into_kernel<T><<<nblk_vec, kBlock, 0, st>>>(n, pb, V, ctl);
+        SPAI_LAUNCH("scale_into_kernel");
+        launches += 4;
+    }
+
+    int read_flag(cudaStream_t st, int *host_flag, const int *dev_flag) {
+        SPAI_CUDA(cudaMemcpyAsync(host_flag, dev_flag, sizeof(int), cudaMemcpyDeviceToHost, st));
+        SPAI_CUDA(cudaStreamSynchronize(st));
+        return *host_flag;
+    }
+
+    // Inner GMRES loop driven from the host in batches of speculative steps (steps after the
+    // solve ends are no-ops gated on ctl->active).
+    void gmres_loop(cudaStream_t st, bool accept_every, int *pinned) {
+        const int batch = 8;
+        for (int it = 0; it < cap; it += batch) {
+            for (int s = 0; s < batch && it + s < cap; ++s)
+                arnoldi_step(st);
+            if (!read_flag(st, pinned, &ctl->active))
+                break;
+        }
+    }
+
+    // One GMRES solve of P A d = P rhs (x0 = 0) on the current contents of `rhs`.
+    void gmres_only(cudaStream_t st, const SolveSettings &s, int *pinned) {
+        launches = 0;
+        Ctl h{};
+        h.cap = cap;
+        h.outer_cap = 0;
+        h.tol_inner = s.tau;
+        h.outer_active = 1;
+        h.ir_status = -1;
+        h.last_gmres_status = -1;
+        h.inner_scale = 1.0;
+        h.nrows = n;
+        h.accept_every = s.accept_every ? 1 : 0;
+        SPAI_CUDA(cudaMemcpyAsync(ctl, &h, sizeof(Ctl), cudaMemcpyHostToDevice, st));
+        SPAI_CUDA(cudaMemsetAsync(counters, 0, 16 * sizeof(int), st));
+        gmres_start(st, s.accept_every);
+        gmres_loop(st, s.accept_every, pinned);
+    }
+
+    // Full refinement solve; b, x are device vectors in TO.
+    void solve(cudaStream_t st, const TO *b, TO *x, const SolveSettings &s, int *pinned) {
+        launches = 0;
+        Ctl h{};
+        h.cap = cap;
+        h.outer_cap = s.outer_cap;
+        h.tol_inner = s.tau;
+        h.be_tol = s.be_tol;
+        h.bscale = s.scale_rhs ? 1.0 : 0.0;
+        h.outer_active = 1;
+        h.ir_status = -1;
+        h.last_gmres_status = -1;
+        h.inner_scale = 1.0;
+        h.nrows = n;
+        h.accept_every = s.accept_every ? 1 : 0;
+        SPAI_CUDA(cudaMemcpyAsync(ctl, &h, sizeof(Ctl), cudaMemcpyHostToDevice, st));
+        SPAI_CUDA(cudaMemsetAsync(counters, 0, 16 * sizeof(int), st));
+        norms_inf_kernel<TO><<<nblk_vec, kBlock, 0, st>>>(n, a_outer->rp, a_outer->val, b, dpart,
+                                                          ctl, counters + kSlotMisc);
+        SPAI_LAUNCH("norms_inf_kernel");
+        ir_x0_kernel<T, TO><<<nblk_vec, kBlock, 0, st>>>(n, p->rp, p->ci, p->val, b, x);
+        SPAI_LAUNCH("ir_x0_kernel");
+        residual(st, b, x);
+        launches += 2;
+        for (int step = 0; step <= s.outer_cap; ++step) {
+            if (!read_flag(st, pinned, &ctl->outer_active))
+                break;
+            make_rhs_kernel<TO, T><<<nblk_vec, kBlock, 0, st>>>(n, r, rhs, ctl);
+            SPAI_LAUNCH("make_rhs_kernel");
+            gmres_start(st, s.accept_every);
+            gmres_loop(st, s.accept_every, pinned);
+            ir_after_inner_kernel<<<1, 32, 0, st>>>(ctl);
+            SPAI_LAUNCH("ir_after_inner_kernel");
+            ir_update_kernel<TO, T><<<nblk_vec, kBlock, 0, st>>>(n, x, xn, cand, ctl);
+            SPAI_LAUNCH("ir_update_kernel");
+            ir_after_update_kernel<<<1, 32, 0, st>>>(ctl);
+            SPAI_LAUNCH("ir_after_update_kernel");
+            residual(st, b, xn);
+            ir_commit_kernel<TO><<<nblk_vec, kBlock, 0, st>>>(n, x, xn, ctl);
+            SPAI_LAUNCH("ir_commit_kernel");
+            launches += 5;
+        }
+    }
+
+    void residual(cudaStream_t st, const TO *b, TO *x) {
+        const int G = pick_group(*a_outer);
+        const unsigned blocks = nblk_vec;
+        switch (G) {
+        case 2:
+            ir_residual_kernel<TO, 2><<<blocks, kBlock, 0, st>>>(n, a_outer->rp, a_outer->ci, a_outer->val, x, b, r, dpart, ctl, counters + kSlotDiag);
+            break;
+        case 4:
+            ir_residual_kernel<TO, 4><<<blocks, kBlock, 0, st>>>(n, a_outer->rp, a_outer->ci, a_outer->val, x, b, r, dpart, ctl, counters + kSlotDiag);
+            break;
+        case 8:
+            ir_residual_kernel<TO, 8><<<blocks, kBlock, 0, st>>>(n, a_outer->rp, a_outer->ci, a_outer->val, x, b, r, dpart, ctl, counters + kSlotDiag);
+            break;
+        case 16:
+            ir_residual_kernel<TO, 16><<<blocks, kBlock, 0, st>>>(n, a_outer->rp, a_outer->ci, a_outer->val, x, b, r, dpart, ctl, counters + kSlotDiag);
+            break;
+        default:
+            ir_residual_kernel<TO, 32><<<blocks, kBlock, 0, st>>>(n, a_outer->rp, a_outer->ci, a_outer->val, x, b, r, dpart, ctl, counters + kSlotDiag);
+        }
+        SPAI_LAUNCH("ir_residual_kernel");
+        ++launches;
+    }
+};
+
+} // namespace spai

@@ -1,0 +1,99 @@
+// Internal interfaces between the library's translation units.
+#pragma once
+#include "common.cuh"
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+#include <vector>
+
+namespace spai {
+
+// Device CSR with 32-bit indices (nnz < 2^31 is checked at upload).
+template <class T> struct DeviceCsr {
+    int n = 0, nnz = 0;
+    int *rp = nullptr, *ci = nullptr;
+    T *val = nullptr;
+};
+
+// Call-sequence caching allocator: the i-th alloc() after a reset() reuses the i-th buffer when
+// it is large enough, so repeated builds/solves of the same shape allocate nothing.
+class DeviceArena {
+  public:
+    DeviceArena() = default;
+    DeviceArena(const DeviceArena &) = delete;
+    DeviceArena &operator=(const DeviceArena &) = delete;
+    ~DeviceArena() {
+        for (auto &s : slots_)
+            if (s.ptr)
+                cudaFree(s.ptr);
+    }
+    void reset() {
+        next_ = 0;
+    }
+    template <class U> U *alloc(size_t count) {
+        const size_t bytes = ((count ? count : 1) * sizeof(U) + 255) & ~size_t(255);
+        if (next_ == slots_.size())
+            slots_.push_back(Slot{});
+        Slot &s = slots_[next_++];
+        if (s.bytes < bytes) {
+            if (s.ptr)
+                SPAI_CUDA(cudaFree(s.ptr));
+            s.ptr = nullptr;
+            s.bytes = 0;
+            SPAI_CUDA(cudaMalloc(&s.ptr, bytes));
+            s.bytes = bytes;
+        }
+        return static_cast<U *>(s.ptr);
+    }
+    size_t bytes_held() const {
+        size_t b = 0;
+        for (auto &s : slots_)
+            b += s.bytes;
+        return b;
+    }
+
+  private:
+    struct Slot {
+        void *ptr = nullptr;
+        size_t bytes = 0;
+    };
+    std::vector<Slot> slots_;
+    size_t next_ = 0;
+};
+
+struct SpaiParams {
+    double epsilon = 0.3;
+    long long alpha = 5;
+    int beta = 8;
+    int ws_bytes_per_warp = 0;   // 0 = tuned default
+    int warps_per_block = 0;     // 0 = tuned default
+    size_t overflow_ws_bytes = 0;
+};
+
+template <class T> struct SpaiOutput {
+    int n = 0;
+    int status = 1;
+    int first_failed = -1;
+    long long fits = 0, growths = 0;
+    int overflow_columns = 0;
+    long long launches = 0;
+    T *d = nullptr;
+    int *col_status = nullptr, *col_fits = nullptr, *col_growths = nullptr, *col_clamps = nullptr,
+        *col_q = nullptr;
+    T *col_residual = nullptr;
+    long long *packed_off = nullptr;
+    int *packed_idx = nullptr;
+    T *packed_val = nullptr;
+    DeviceCsr<T> p; // P = N^T D
+};
+
+template <class T> struct SpaiBuilder {
+    static void construct(const DeviceCsr<T> &a, const SpaiParams &prm, cudaStream_t st,
+                          SpaiOutput<T> &out, DeviceArena &arena);
+};
+
+template <class T> void score_kat(T rsq, T dot, T den, double *out);
+
+} // namespace spai

@@ -1,0 +1,294 @@
+"""Python mirror of the libspai_ir C ABI (include/spai_ir.h).
+
+Names and semantics follow the reference's solver API (include/bspai/*.hpp): the status enums
+and their names, SpaiOptions/GmresOptions/IrOptions defaults, cuda_gpu_spai_gmres_ir as
+ir_solve(), CudaGmresContext as Handle.gmres(), CudaCsrSpmv as Handle.spmv(). There is no CPU
+fallback: loading fails loudly when the CUDA library has not been built.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIB_PATH = os.path.join(PKG, "_build", "libspai_ir.so")
+CLI_DIR = os.path.join(PKG, "_build")
+
+PRECISION = {"f64": 0, "f32": 1, "mixed": 2}
+FLAG_NO_GRAPH = 1
+
+SPAI_STATUS = ["success", "not_attempted", "invalid_input", "rank_deficient", "numerical_failure",
+               "empty_candidates", "zero_denominator", "invalid_score", "no_growth", "iteration_limit"]
+GMRES_STATUS = ["success", "zero_rhs", "exact_initial_solution", "invalid_input",
+                "zero_preconditioned_rhs", "breakdown", "iteration_limit", "nonconvergence",
+                "numerical_failure"]
+IR_STATUS = ["success", "invalid_input", "construction_failure", "inner_failure", "stagnation",
+             "iteration_limit", "numerical_failure"]
+
+OK, ERR_ARGUMENT, ERR_CUDA, ERR_WORKSPACE, ERR_TIMEOUT, ERR_NOT_BUILT, ERR_UNSUPPORTED = 0, -1, -2, -3, -4, -5, -6
+
+
+class SpaiError(RuntimeError):
+    def __init__(self, code, message):
+        super().__init__(f"libspai_ir error {code}: {message}")
+        self.code = code
+
+
+class Csr(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_int64), ("nnz", ctypes.c_int64),
+                ("row_offsets", ctypes.POINTER(ctypes.c_int64)),
+                ("col_indices", ctypes.POINTER(ctypes.c_int64)),
+                ("values", ctypes.POINTER(ctypes.c_double))]
+
+
+class Options(ctypes.Structure):
+    _fields_ = [("epsilon", ctypes.c_double), ("alpha", ctypes.c_int64), ("beta", ctypes.c_int64),
+                ("tau", ctypes.c_double), ("innercap", ctypes.c_int64), ("outercap", ctypes.c_int64),
+                ("be_tolerance", ctypes.c_double), ("precision", ctypes.c_int32),
+                ("flags", ctypes.c_int32)]
+
+
+class Report(ctypes.Structure):
+    _fields_ = [("ir_status", ctypes.c_int32), ("spai_status", ctypes.c_int32),
+                ("gmres_status", ctypes.c_int32), ("converged", ctypes.c_int32),
+                ("outer_steps", ctypes.c_int64), ("inner_attempts", ctypes.c_int64),
+                ("inner_iterations", ctypes.c_int64), ("nnz_p", ctypes.c_int64),
+                ("first_failed_column", ctypes.c_int64), ("backward_error", ctypes.c_double),
+                ("componentwise_backward_error", ctypes.c_double), ("residual_inf", ctypes.c_double),
+                ("forward_error", ctypes.c_double), ("spai_ms", ctypes.c_double),
+                ("solve_ms", ctypes.c_double), ("spai_fits", ctypes.c_int64),
+                ("spai_growths", ctypes.c_int64), ("spai_overflow_columns", ctypes.c_int64),
+                ("kernel_launches", ctypes.c_int64)]
+
+    def as_dict(self):
+        d = {name: getattr(self, name) for name, _ in self._fields_}
+        d["converged"] = bool(d["converged"])
+        return d
+
+
+I64P = ctypes.POINTER(ctypes.c_int64)
+I32P = ctypes.POINTER(ctypes.c_int32)
+F64P = ctypes.POINTER(ctypes.c_double)
+VP = ctypes.c_void_p
+
+# Every exported entry point of include/spai_ir.h with its ctypes signature.
+SIGNATURES = {
+    "spai_default_options": (ctypes.c_int, [ctypes.POINTER(Options), ctypes.c_int32]),
+    "spai_status_name": (ctypes.c_char_p, [ctypes.c_int32]),
+    "gmres_status_name": (ctypes.c_char_p, [ctypes.c_int32]),
+    "ir_status_name": (ctypes.c_char_p, [ctypes.c_int32]),
+    "spai_last_error": (ctypes.c_char_p, []),
+    "spai_create": (ctypes.c_int, [ctypes.POINTER(Csr), ctypes.c_int32, ctypes.c_int, VP, ctypes.POINTER(VP)]),
+    "spai_destroy": (ctypes.c_int, [VP]),
+    "spai_build": (ctypes.c_int, [VP, ctypes.POINTER(Options), ctypes.POINTER(Report)]),
+    "spai_solve": (ctypes.c_int, [VP, F64P, F64P, F64P, ctypes.POINTER(Options), ctypes.POINTER(Report)]),
+    "spai_solve_device": (ctypes.c_int, [VP, VP, VP, ctypes.POINTER(Options), ctypes.POINTER(Report)]),
+    "spai_ir_solve": (ctypes.c_int, [ctypes.POINTER(Csr), F64P, F64P, F64P, ctypes.POINTER(Options),
+                                     ctypes.POINTER(Report), VP]),
+    "spai_get_preconditioner": (ctypes.c_int, [VP, I64P, I64P, I64P, F64P]),
+    "spai_get_columns": (ctypes.c_int, [VP, I32P, I32P, I32P, I32P, F64P, F64P]),
+    "spai_get_column": (ctypes.c_int, [VP, ctypes.c_int64, I64P, I64P, F64P]),
+    "spai_spmv": (ctypes.c_int, [VP, ctypes.c_int32, F64P, F64P]),
+    "spai_gmres": (ctypes.c_int, [VP, F64P, F64P, ctypes.c_double, ctypes.c_int64, I32P, I64P, F64P]),
+    "spai_score": (ctypes.c_int, [ctypes.c_int32, ctypes.c_double, ctypes.c_double, ctypes.c_double, F64P]),
+    "spai_ir_solve_batched": (ctypes.c_int, [ctypes.c_int64, ctypes.POINTER(Csr), ctypes.POINTER(F64P),
+                                             ctypes.POINTER(F64P), ctypes.POINTER(Options),
+                                             ctypes.POINTER(Report), VP]),
+    "spai_adjoint": (ctypes.c_int, [VP, ctypes.c_int64, F64P, F64P, F64P, F64P, ctypes.POINTER(Options),
+                                    ctypes.POINTER(Report)]),
+    "spai_hypot": (ctypes.c_double, [ctypes.c_double, ctypes.c_double]),
+    "spai_hypotf": (ctypes.c_float, [ctypes.c_float, ctypes.c_float]),
+}
+
+_lib = None
+
+
+def lib():
+    """Load the in-tree CUDA library; raises if it has not been built (no CPU fallback)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"libspai_ir.so not built at {LIB_PATH}; run __graft_entry__.build()")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _check(rc):
+    if rc != OK:
+        raise SpaiError(rc, lib().spai_last_error().decode())
+
+
+def _p(a, t):
+    return a.ctypes.data_as(t)
+
+
+class _CsrHolder:
+    """Keeps the int64/float64 arrays of a canonical CSR alive while C holds pointers to them."""
+
+    def __init__(self, system):
+        n, ptr, idx, val = system
+        self.ptr = np.ascontiguousarray(ptr, np.int64)
+        self.idx = np.ascontiguousarray(idx, np.int64)
+        self.val = np.ascontiguousarray(val, np.float64)
+        self.n = int(n)
+        self.csr = Csr(self.n, len(self.val), _p(self.ptr, I64P), _p(self.idx, I64P), _p(self.val, F64P))
+
+
+def options(precision="f64", epsilon=0.3, alpha=5, beta=8, tau=0.0, innercap=0, outercap=20,
+            be_tolerance=0.0, flags=0):
+    """IrOptions with the reference defaults (spai.hpp:24-28, gmres.hpp:23-26, ir.hpp:20-24)."""
+    o = Options()
+    _check(lib().spai_default_options(ctypes.byref(o), PRECISION[precision]))
+    o.epsilon, o.alpha, o.beta, o.tau = epsilon, alpha, beta, tau
+    o.innercap, o.outercap, o.be_tolerance, o.flags = innercap, outercap, be_tolerance, flags
+    return o
+
+
+def cli_options(n, precision="f64", epsilon=0.3, outercap=20, innercap=0, **kw):
+    """Options the drop-in CLI uses: alpha = ceil(n/8), beta = 8 (src/solver_main.cpp:75-76)."""
+    return options(precision, epsilon=epsilon, alpha=(n + 7) // 8, beta=8, outercap=outercap,
+                   innercap=innercap, **kw)
+
+
+class Handle:
+    """Device-resident matrix, SPAI preconditioner and Krylov workspace (spai_handle)."""
+
+    def __init__(self, system, precision="f64", device=0, stream=None):
+        self.precision = precision
+        self._csr = _CsrHolder(system)
+        self.n = self._csr.n
+        h = VP()
+        _check(lib().spai_create(ctypes.byref(self._csr.csr), PRECISION[precision], device, stream,
+                                 ctypes.byref(h)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().spai_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def build(self, opts):
+        rep = Report()
+        _check(lib().spai_build(self._h, ctypes.byref(opts), ctypes.byref(rep)))
+        return rep.as_dict()
+
+    def solve(self, b, opts, reference=None):
+        b = np.ascontiguousarray(b, np.float64)
+        x = np.zeros(self.n)
+        ref = None if reference is None else np.ascontiguousarray(reference, np.float64)
+        rep = Report()
+        _check(lib().spai_solve(self._h, _p(b, F64P), _p(x, F64P), None if ref is None else _p(ref, F64P),
+                                ctypes.byref(opts), ctypes.byref(rep)))
+        return x, rep.as_dict()
+
+    def solve_device(self, b_ptr, x_ptr, opts):
+        rep = Report()
+        _check(lib().spai_solve_device(self._h, VP(b_ptr), VP(x_ptr), ctypes.byref(opts), ctypes.byref(rep)))
+        return rep.as_dict()
+
+    def preconditioner(self):
+        nnz = ctypes.c_int64()
+        _check(lib().spai_get_preconditioner(self._h, ctypes.byref(nnz), None, None, None))
+        ptr = np.zeros(self.n + 1, np.int64)
+        idx = np.zeros(nnz.value, np.int64)
+        val = np.zeros(nnz.value)
+        _check(lib().spai_get_preconditioner(self._h, ctypes.byref(nnz), _p(ptr, I64P), _p(idx, I64P), _p(val, F64P)))
+        return (self.n, ptr, idx, val)
+
+    def columns(self):
+        n = self.n
+        st, fi, gr, cl = (np.zeros(n, np.int32) for _ in range(4))
+        res, sc = np.zeros(n), np.zeros(n)
+        _check(lib().spai_get_columns(self._h, _p(st, I32P), _p(fi, I32P), _p(gr, I32P), _p(cl, I32P),
+                                      _p(res, F64P), _p(sc, F64P)))
+        return dict(status=st, fits=fi, growths=gr, clamps=cl, residual=res, scaling=sc)
+
+    def column(self, k):
+        q = ctypes.c_int64()
+        _check(lib().spai_get_column(self._h, k, ctypes.byref(q), None, None))
+        pat = np.zeros(q.value, np.int64)
+        coef = np.zeros(q.value)
+        _check(lib().spai_get_column(self._h, k, ctypes.byref(q), _p(pat, I64P), _p(coef, F64P)))
+        return pat, coef
+
+    def spmv(self, which, x):
+        x = np.ascontiguousarray(x, np.float64)
+        y = np.zeros(self.n)
+        _check(lib().spai_spmv(self._h, {"A": 0, "P": 1}[which], _p(x, F64P), _p(y, F64P)))
+        return y
+
+    def gmres(self, rhs, tau, cap=0):
+        rhs = np.ascontiguousarray(rhs, np.float64)
+        x = np.zeros(self.n)
+        st, it, rel = ctypes.c_int32(), ctypes.c_int64(), ctypes.c_double()
+        _check(lib().spai_gmres(self._h, _p(rhs, F64P), _p(x, F64P), tau, cap, ctypes.byref(st),
+                                ctypes.byref(it), ctypes.byref(rel)))
+        return x, dict(status=st.value, iterations=it.value, final_relative=rel.value)
+
+    def adjoint(self, x, dldx, opts):
+        x = np.asfortranarray(x, np.float64)
+        dldx = np.asfortranarray(dldx, np.float64)
+        nrhs = 1 if x.ndim == 1 else x.shape[1]
+        dldb = np.zeros_like(dldx)
+        dlda = np.zeros(len(self._csr.val))
+        rep = Report()
+        _check(lib().spai_adjoint(self._h, nrhs, _p(x, F64P), _p(dldx, F64P), _p(dldb, F64P), _p(dlda, F64P),
+                                  ctypes.byref(opts), ctypes.byref(rep)))
+        return dldb, dlda, rep.as_dict()
+
+
+def ir_solve(system, b, opts, reference=None, stream=None):
+    """One-shot solve (cuda_gpu_spai_gmres_ir / fp32_cuda_spai_gmres_ir): returns (x, report)."""
+    holder = _CsrHolder(system)
+    b = np.ascontiguousarray(b, np.float64)
+    x = np.zeros(holder.n)
+    ref = None if reference is None else np.ascontiguousarray(reference, np.float64)
+    rep = Report()
+    _check(lib().spai_ir_solve(ctypes.byref(holder.csr), _p(b, F64P), _p(x, F64P),
+                               None if ref is None else _p(ref, F64P), ctypes.byref(opts),
+                               ctypes.byref(rep), stream))
+    return x, rep.as_dict()
+
+
+def ir_solve_batched(systems, bs, opts, stream=None):
+    holders = [_CsrHolder(s) for s in systems]
+    arr = (Csr * len(holders))(*[h.csr for h in holders])
+    bs = [np.ascontiguousarray(b, np.float64) for b in bs]
+    xs = [np.zeros(h.n) for h in holders]
+    bp = (F64P * len(bs))(*[_p(b, F64P) for b in bs])
+    xp = (F64P * len(xs))(*[_p(x, F64P) for x in xs])
+    reps = (Report * len(holders))()
+    _check(lib().spai_ir_solve_batched(len(holders), arr, bp, xp, ctypes.byref(opts), reps, stream))
+    return xs, [r.as_dict() for r in reps]
+
+
+def score(rsq, dot, den, precision="f64"):
+    out = np.zeros(3)
+    _check(lib().spai_score(PRECISION[precision], rsq, dot, den, _p(out, F64P)))
+    return int(out[0]), float(out[1]), bool(out[2])
+
+
+def hypot(a, b):
+    return lib().spai_hypot(a, b)
+
+
+def hypotf(a, b):
+    return lib().spai_hypotf(a, b)
+
+
+def cli_path(name):
+    return os.path.join(CLI_DIR, name)

@@ -1,0 +1,59 @@
+"""First GPU parity checks through the C ABI (SPAI bitwise vs oracle, IR vs oracle)."""
+import numpy as np
+import pytest
+
+import oracle as O
+import spai_ir
+from spai_ir import matrices as M
+from conftest import golden, golden_system
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("name", ["tiny", "band64_5", "cd2d_32", "cd3d_12", "aniso_24"])
+@pytest.mark.parametrize("prec", ["f64", "f32"])
+def test_spai_bitwise_vs_oracle(built, name, prec):
+    g = golden(name)
+    system = golden_system(g)
+    eps, alpha, beta = g["spai_args"]
+    opts = spai_ir.options("mixed" if prec == "f32" else "f64", epsilon=eps, alpha=int(alpha), beta=int(beta))
+    with spai_ir.Handle(system, "mixed" if prec == "f32" else "f64") as h:
+        rep = h.build(opts)
+        p = h.preconditioner()
+        cols = h.columns()
+    ref = O.Spai(system, eps, int(alpha), int(beta), precision=prec)
+    assert rep["spai_status"] == ref.status
+    assert np.array_equal(cols["status"], ref.col_status)
+    assert np.array_equal(cols["fits"], ref.fits)
+    assert np.array_equal(p[1], ref.p_ptr) and np.array_equal(p[2], ref.p_idx)
+    assert np.array_equal(p[3], ref.p_val)
+
+
+@pytest.mark.parametrize("name", ["tiny", "band256_8", "cd2d_64", "cd3d_12", "aniso_24", "irregular_3000"])
+def test_ir_f64_vs_oracle(built, name):
+    g = golden(name)
+    system = golden_system(g)
+    n = system[0]
+    eps, alpha, beta = g["spai_args"]
+    b = M.equal_rhs(n)
+    opts = spai_ir.options("f64", epsilon=eps, alpha=int(alpha), beta=int(beta))
+    x, rep = spai_ir.ir_solve(system, b, opts)
+    xo, ro = O.ir(system, b, epsilon=eps, alpha=int(alpha), beta=int(beta))
+    assert rep["ir_status"] == ro["status"] == 0
+    assert rep["backward_error"] <= 10 * 2.0 ** -53
+    assert rep["outer_steps"] == ro["outer_steps"]
+    assert np.max(np.abs(x - xo)) <= 1e-12 * np.max(np.abs(xo)) * max(1, np.linalg.cond(M.dense(system)) if n <= 600 else 1e3)
+
+
+@pytest.mark.parametrize("prec", ["mixed", "f32"])
+def test_ir_lower_precisions(built, prec):
+    system = M.convection_diffusion_2d(32)
+    n = system[0]
+    b = M.equal_rhs(n)
+    opts = spai_ir.cli_options(n, prec)
+    x, rep = spai_ir.ir_solve(system, b, opts)
+    assert rep["converged"], rep
+    if prec == "mixed":
+        assert rep["backward_error"] <= 10 * 2.0 ** -53
+    else:
+        assert rep["backward_error"] <= 10 * 2.0 ** -24
