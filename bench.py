@@ -1,0 +1,373 @@
+"""Benchmark: SPAI-GMRES-IR solve time to normwise backward error <= 1e-12 on GB300.
+
+Workload (one "step" = one complete solve of one system): the 3-D convection-diffusion system
+on a 128^3 grid (n = 2,097,152, 7-point first-order upwind, velocity (1,1,1)/sqrt(3), cell
+Peclet 5, nnz 14,581,760; seeded synthetic, generated by spai_ir.matrices), equal-component
+unit-norm right-hand side, epsilon 0.3, alpha ceil(n/8), beta 8, innercap 200, outercap 20,
+mixed precision (SPAI and GMRES in binary32, refinement residual/update/norms in binary64).
+The plain binary64 form on the same system is timed beside it.
+
+value : device time per solve (SPAI build + refinement) with A and b already in HBM (CUDA events
+        on the solve stream, synchronised on both sides). Inputs exceed L2 (A alone 175 MB).
+e2e   : the same solve through the C ABI with host buffers: spai_ir_solve uploads the host CSR and
+        b, builds, solves and copies x back, all inside the timed region.
+roofline: the dominant HBM-bound kernel class of the solve (CUDA-event time per launch over an
+        instrumented solve, algorithmic bytes per launch from the matrix/basis sizes).
+cpu_baseline: the CPU oracle (this repository's restatement of the reference algorithm) on a
+        bounded sample: SPAI fits of a column sample on all host threads, and fixed-length GMRES
+        runs on one thread, extrapolated to the GPU run's fit and iteration counts.
+
+--impl reference runs the reference's CPU path on the host cores instead (the oracle port: the
+reference's own sources are not present on the GPU host), for the same workload and metric.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "spai-gmres-ir_gb300"))
+
+METRIC = "solve time at backward err <=1e-12: mixed FP32/64 vs plain FP64 on GB300; HBM GB/s"
+BE_TARGET = 1e-12
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--grid", type=int, default=128, help="cube side (128 = the benchmark system)")
+    ap.add_argument("--innercap", type=int, default=200)
+    ap.add_argument("--fp64-steps", type=int, default=1)
+    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--profile-run", choices=["mixed", "f64"], default=None,
+                    help="one untimed build+solve of the workload (a clean launch sequence for ncu)")
+    return ap.parse_args()
+
+
+def profile_run(args):
+    import spai_ir
+    from spai_ir import matrices as M
+
+    system = M.convection_diffusion_3d(args.grid)
+    n = system[0]
+    opts = spai_ir.cli_options(n, args.profile_run, innercap=args.innercap, be_tolerance=BE_TARGET)
+    with spai_ir.Handle(system, args.profile_run) as h:
+        rb = h.build(opts)
+        x, rs = h.solve(M.equal_rhs(n), opts)
+    print(json.dumps({"profile_run": args.profile_run, "n": n, "spai_ms": rb["spai_ms"],
+                      "solve_ms": rs["solve_ms"], "outer": rs["outer_steps"],
+                      "inner": rs["inner_iterations"], "be": rs["backward_error"]}))
+
+
+def max_over_ranks(value, world):
+    """Max of a per-rank timing over the process group (nccl on GPUs, gloo on CPU)."""
+    if world <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+
+    dev = (torch.device("cuda", torch.cuda.current_device()) if dist.get_backend() == "nccl"
+           else torch.device("cpu"))
+    t = torch.tensor([float(value)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region (SM clock, max clock, throttle reasons)."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.QUERY,
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True,
+                                     timeout=5).stdout.strip()
+                if out:
+                    self.samples.append([c.strip() for c in out.split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in self.samples if s[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for s in self.samples:
+            for i, nm in enumerate(names):
+                if len(s) > 5 + i and s[5 + i].lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.samples)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profile_traffic():
+    """DRAM bytes per launch of the dominant kernel from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(path) as f:
+            return json.load(f)
+    except Exception:
+        return None
+
+
+def run_ours(args, rank, world, local):
+    import numpy as np
+    import torch
+
+    import spai_ir
+    from spai_ir import matrices as M
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.Stream(device=dev)  # the library launches on this stream
+    system = M.convection_diffusion_3d(args.grid)
+    n, ptr, idx, val = system
+    b_host = M.equal_rhs(n)
+    opts = {p: spai_ir.cli_options(n, p, innercap=args.innercap, be_tolerance=BE_TARGET)
+            for p in ("mixed", "f64")}
+    b_dev = torch.from_numpy(b_host).to(dev)
+    x_dev = torch.zeros(n, dtype=torch.float64, device=dev)
+    torch.cuda.synchronize()
+    handles = {p: spai_ir.Handle(system, p, device=local, stream=stream.cuda_stream)
+               for p in ("mixed",) + (() if args.no_fp64 else ("f64",))}
+
+    def step(p):
+        h = handles[p]
+        rb = h.build(opts[p])
+        rs = h.solve_device(b_dev.data_ptr(), x_dev.data_ptr(), opts[p])
+        return rb, rs
+
+    def timed(p, steps, warmup):
+        for _ in range(warmup):
+            step(p)
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        launches = 0
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(steps):
+            rb, rs = step(p)
+            launches += rb["kernel_launches"] + rs["kernel_launches"]
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = max_over_ranks(e0.elapsed_time(e1) / steps, world)
+        return ms, rb, rs, launches
+
+    with Clocks(local) as clocks:
+        ms_mixed, rb_m, rs_m, launches = timed("mixed", args.steps, args.warmup)
+    # Correctness of the timed result against the stop rule.
+    xm = x_dev.cpu().numpy()
+    assert rs_m["converged"] and rs_m["backward_error"] <= BE_TARGET, rs_m
+
+    # End-to-end through the public C ABI with host buffers (upload A and b, copy x back).
+    e2e_ms = []
+    for i in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        x, r = spai_ir.ir_solve(system, b_host, opts["mixed"], stream=stream.cuda_stream)
+        t1 = time.perf_counter()
+        if i >= args.warmup:
+            e2e_ms.append((t1 - t0) * 1e3)
+        assert r["converged"], r
+    e2e = statistics.median(e2e_ms)
+    h2d = (n + 1) * 8 + len(val) * 16 + n * 8
+    d2h = n * 8
+
+    # Plain binary64 on the same system (fewer repetitions: its SPAI runs on the FP64 pipe).
+    fp64 = None
+    if not args.no_fp64:
+        ms64, rb64, rs64, _ = timed("f64", args.fp64_steps, 1)
+        fp64 = {"ms_per_solve": ms64, "spai_ms": rb64["spai_ms"], "solve_ms": rs64["solve_ms"],
+                "outer_steps": rs64["outer_steps"], "inner_iterations": rs64["inner_iterations"],
+                "backward_error": rs64["backward_error"]}
+        x64 = x_dev.cpu().numpy()
+        fp64["mixed_vs_fp64_forward"] = float(np.max(np.abs(xm - x64)) / np.max(np.abs(x64)))
+
+    # Roofline of the dominant HBM-bound kernel class from an instrumented solve.
+    h = handles["mixed"]
+    h.profile(True)
+    h.solve_device(b_dev.data_ptr(), x_dev.data_ptr(), opts["mixed"])
+    prof = h.profile_read()
+    h.profile(False)
+    dom = max(prof, key=lambda k: prof[k]["ms"])
+    peak, peak_kind = measured_peaks()
+    d = prof[dom]
+    achieved = d["bytes"] / (d["ms"] * 1e-3) / 1e9 if d["ms"] > 0 else 0.0
+    traffic = None
+    tr = profile_traffic()
+    if tr and tr.get("kernel_class") == dom:
+        traffic = tr.get("dram_bytes_per_launch")
+    roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "traffic": traffic, "kernel": dom,
+                "peak_source": peak_kind,
+                "bytes_per_launch": d["bytes"] / max(d["launches"], 1),
+                "ms_per_launch": d["ms"] / max(d["launches"], 1), "launches": d["launches"],
+                "classes": {k: {"ms": round(v["ms"], 3), "GB/s": round(v["bytes"] / (v["ms"] * 1e-3) / 1e9, 1)
+                                if v["ms"] > 0 else 0.0} for k, v in prof.items()}}
+    p_mixed = handles["mixed"].preconditioner()
+    for hh in handles.values():
+        hh.close()
+    return {"p": p_mixed, "ms": ms_mixed, "rb": rb_m, "rs": rs_m, "launches": launches, "e2e": e2e, "h2d": h2d,
+            "d2h": d2h, "fp64": fp64, "roofline": roofline, "clocks": clocks.summary(), "n": n,
+            "nnz": len(val)}
+
+
+def cpu_estimate(grid, fits_total, iter_counts, threads, precision="mixed", p_system=None):
+    """Oracle cost on a bounded sample, extrapolated to the full solve."""
+    import numpy as np
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    from spai_ir import matrices as M
+
+    system = M.convection_diffusion_3d(grid)
+    n = system[0]
+    rng = np.random.default_rng(0)
+    cols = np.sort(rng.choice(n, size=min(n, 32768), replace=False))
+    sec, fits = O.spai_sample_seconds(system, cols, epsilon=0.3, alpha=(n + 7) // 8, beta=8,
+                                      precision=precision, threads=threads)
+    spai_total = sec / len(cols) * n
+    # GMRES cost model t(K) = a K + b K^2 / 2 from two fixed-length runs (tau = 1e-30, so every
+    # step runs). The per-step cost depends on nnz(P), not on P's values: the binary32 SPAI built
+    # on the GPU (bit-identical to the oracle's) is used when available, else A's pattern stands in.
+    p_like = p_system if p_system is not None else (n, system[1], system[2], system[3] / np.max(np.abs(system[3])))
+    rhs = M.equal_rhs(n)
+    times = {}
+    for K in (4, 12):
+        t0 = time.perf_counter()
+        O.gmres(system, p_like, rhs, tol=1e-30, cap=K, precision="f32" if precision != "f64" else "f64")
+        times[K] = time.perf_counter() - t0
+    b = 2 * (times[12] - 3 * times[4]) / (12 * 12 - 3 * 4 * 4)
+    a = (times[4] - b * 16 / 2) / 4
+    gmres_total = sum(a * K + b * K * K / 2 for K in iter_counts)
+    sample = (f"oracle {precision}: SPAI fits of {len(cols)} sampled columns on {threads} threads "
+              f"({sec:.2f} s, scaled to n={n}); GMRES fixed runs of 4 and 12 steps on 1 thread fitted "
+              f"to a K + b K^2/2 and summed over the GPU run's inner iteration counts {iter_counts}")
+    return (spai_total + gmres_total) * 1e3, sample, {"spai_s": spai_total, "gmres_s": gmres_total}
+
+
+def main():
+    args = parse()
+    if args.profile_run:
+        profile_run(args)
+        return
+    rank, world, local = dist_env()
+    if world > 1 and args.impl == "ours":
+        import torch
+
+        torch.distributed.init_process_group("nccl")
+    threads = os.cpu_count() or 1
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        iters = [110, 150, 150, 150]
+        ms_list = []
+        for _ in range(max(1, min(args.steps, 2))):
+            ms, sample, parts = cpu_estimate(args.grid, 0, iters, threads)
+            ms_list.append(ms)
+        ms = statistics.median(ms_list)
+        line = {"impl": "reference", "metric": METRIC, "value": round(ms, 1), "unit": "ms",
+                "n_gpus": args.gpus, "steps": len(ms_list), "warmup": 0, "ms_per_step": round(ms, 1),
+                "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+                "data": "synthetic (seeded 128^3 upwind convection-diffusion)",
+                "config": {"workload": "mixed SPAI-GMRES-IR, 3-D convection-diffusion 128^3 (n=2097152, "
+                                       "nnz=14581760), eps 0.3, innercap 200, outercap 20, BE<=1e-12",
+                           "l2": "inputs larger than L2"},
+                "cpu_baseline": {"value": round(ms, 1), "unit": "ms", "cores": threads, "kind": "port",
+                                 "sample": sample},
+                "e2e": {"value": round(ms, 1), "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+                "note": "reference sources are absent on the GPU host; the oracle restatement of the "
+                        "reference CPU algorithm is timed (the reference's own O(n^2) CPU SPAI would "
+                        "take days at this size)"}
+        print(json.dumps(line))
+        return
+    res = run_ours(args, rank, world, local)
+    if world > 1:
+        import torch
+
+        torch.distributed.barrier()
+    if rank != 0:
+        return
+    cpu = None
+    if not args.no_cpu:
+        iters_est = [res["rs"]["inner_iterations"] // max(res["rs"]["inner_attempts"], 1)] * max(
+            res["rs"]["inner_attempts"], 1)
+        ms_cpu, sample, parts = cpu_estimate(args.grid, res["rb"]["spai_fits"], iters_est, threads,
+                                             p_system=res["p"])
+        cpu = {"value": round(ms_cpu, 1), "unit": "ms", "cores": threads, "kind": "port", "sample": sample}
+    line = {
+        "metric": METRIC, "value": round(res["ms"], 2), "unit": "ms", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(res["ms"], 2),
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+        "data": "synthetic (seeded 128^3 upwind convection-diffusion, matrices.py)",
+        "config": {"workload": "mixed SPAI-GMRES-IR, 3-D convection-diffusion %d^3 (n=%d, nnz=%d), eps 0.3, "
+                               "alpha ceil(n/8), beta 8, innercap %d, outercap 20, BE<=1e-12"
+                               % (args.grid, res["n"], res["nnz"], args.innercap),
+                   "parallelism": "replicas" if world > 1 else "single GPU",
+                   "l2": "inputs larger than L2 (A 175 MB, Krylov basis GBs); no flush"},
+        "e2e": {"value": round(res["e2e"], 2), "unit": "ms", "h2d_bytes_per_step": res["h2d"],
+                "d2h_bytes_per_step": res["d2h"]},
+        "gpu_launches": int(res["launches"]),
+        "roofline": res["roofline"],
+        "cpu_baseline": cpu,
+        "clocks": res["clocks"],
+        "solve": {"spai_ms": round(res["rb"]["spai_ms"], 2), "refine_ms": round(res["rs"]["solve_ms"], 2),
+                  "outer_steps": res["rs"]["outer_steps"], "inner_iterations": res["rs"]["inner_iterations"],
+                  "backward_error": res["rs"]["backward_error"], "nnz_p": res["rb"]["nnz_p"]},
+    }
+    if res["fp64"]:
+        line["fp64"] = {k: (round(v, 3) if isinstance(v, float) and abs(v) > 1e-3 else v)
+                        for k, v in res["fp64"].items()}
+        line["mixed_speedup_vs_fp64"] = round(res["fp64"]["ms_per_solve"] / res["ms"], 3)
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

@@ -193,6 +193,14 @@ int spai_ir_solve_batched(int64_t count, const spai_csr *systems, const double *
 int spai_adjoint(spai_handle *h, int64_t nrhs, const double *x, const double *dLdx,
                  double *dLdb, double *dLdA_values, const spai_options *opt, spai_report *rep);
 
+/* Per-kernel-class timing of refinement solves (CUDA events on the handle's stream around each
+ * launch). Classes: 0 SpMV with A, 1 SpMV with P, 2 Gram-Schmidt dot pass, 3 Gram-Schmidt update
+ * pass, 4 normalisation. enable != 0 resets and starts recording; read returns the accumulated
+ * device milliseconds, launch count and algorithmic bytes of one class. No reference
+ * counterpart (the reference only kept host wall-clock telemetry, src/cuda_spai.cu:19-38). */
+int spai_profile(spai_handle *h, int32_t enable);
+int spai_profile_read(spai_handle *h, int32_t cls, double *ms, int64_t *launches, double *bytes);
+
 /* Host builds of the device hypot used by the SPAI fits (parity tests). */
 double spai_hypot(double a, double b);
 float spai_hypotf(float a, float b);

@@ -47,6 +47,10 @@ def lib():
                                    F64P, F64P]
         L.oracle_ir.restype = ctypes.c_int
         L.oracle_ir.argtypes = [ctypes.c_int, ctypes.c_int64, I64P, I64P, F64P, F64P, F64P, F64P, F64P, F64P]
+        L.oracle_spai_sample.restype = ctypes.c_double
+        L.oracle_spai_sample.argtypes = [ctypes.c_int, ctypes.c_int64, I64P, I64P, F64P, ctypes.c_double,
+                                         ctypes.c_int64, ctypes.c_int64, I64P, ctypes.c_int64, ctypes.c_int,
+                                         I64P]
         L.oracle_refine.restype = ctypes.c_int
         L.oracle_refine.argtypes = [ctypes.c_int64, I64P, I64P, F64P, I64P, I64P, F64P, F64P, F64P,
                                     F64P, F64P, F64P]
@@ -194,6 +198,17 @@ def gmres(system, p_system, rhs, tol=1e-8, cap=0, precision="f64", accept_every=
     d = dict(zip(GMRES_KEYS, rep.tolist()))
     d["status"], d["converged"], d["iterations"] = int(d["status"]), bool(d["converged"]), int(d["iterations"])
     return x, d
+
+
+def spai_sample_seconds(system, cols, epsilon=0.3, alpha=5, beta=8, precision="f64", threads=1):
+    """Wall seconds of the oracle's adaptive fits for the given columns (threads in parallel)."""
+    n, ptr, idx, val = _csr(system)
+    cols = np.ascontiguousarray(cols, np.int64)
+    fits = ctypes.c_int64()
+    sec = lib().oracle_spai_sample(1 if precision in ("f32", "mixed") else 0, n, _p(ptr, I64P), _p(idx, I64P),
+                                   _p(val, F64P), epsilon, alpha, beta, _p(cols, I64P), len(cols), threads,
+                                   ctypes.byref(fits))
+    return sec, fits.value
 
 
 def hypot(a, b):

@@ -22,8 +22,10 @@
 #include <cstdint>
 #include <cstring>
 #include <limits>
+#include <chrono>
 #include <numeric>
 #include <stdexcept>
+#include <thread>
 #include <vector>
 
 namespace orc {
@@ -904,6 +906,55 @@ Csr<float> to_float(const Csr<double> &a) {
 
 } // namespace orc
 
+// CPU-baseline sample: time the adaptive fits of the listed columns (construct_column), split
+// over nthreads threads (columns are independent). Returns wall seconds of the fits only;
+// fits_out receives the summed fit count.
+namespace orc {
+template <class T>
+double spai_sample(const Csr<T> &a, const SpaiOptions &o, const int64_t *cols, int64_t ncols,
+                   int nthreads, int64_t *fits_out) {
+    SpaiInput<T> in;
+    in.a = &a;
+    const int64_t n = a.n;
+    in.d.resize(n);
+    for (int64_t r = 0; r < n; ++r) {
+        T mx = 0;
+        for (int64_t e = a.ptr[r]; e < a.ptr[r + 1]; ++e)
+            mx = std::max(mx, std::fabs(a.val[e]));
+        in.d[r] = T(1) / mx;
+    }
+    in.tptr.assign(n + 1, 0);
+    for (int64_t e = 0; e < a.nnz(); ++e)
+        ++in.tptr[a.idx[e] + 1];
+    for (int64_t i = 0; i < n; ++i)
+        in.tptr[i + 1] += in.tptr[i];
+    in.tidx.resize(a.nnz());
+    std::vector<int64_t> fill(in.tptr.begin(), in.tptr.end() - 1);
+    for (int64_t r = 0; r < n; ++r)
+        for (int64_t e = a.ptr[r]; e < a.ptr[r + 1]; ++e)
+            in.tidx[fill[a.idx[e]]++] = r;
+    if (nthreads < 1)
+        nthreads = 1;
+    std::vector<int64_t> fits(nthreads, 0);
+    const auto t0 = std::chrono::steady_clock::now();
+    std::vector<std::thread> pool;
+    for (int t = 0; t < nthreads; ++t)
+        pool.emplace_back([&, t] {
+            for (int64_t i = t; i < ncols; i += nthreads)
+                fits[t] += construct_column(in, cols[i], o, false).fits;
+        });
+    for (auto &th : pool)
+        th.join();
+    const double sec = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    int64_t f = 0;
+    for (int64_t x : fits)
+        f += x;
+    *fits_out = f;
+    return sec;
+}
+
+} // namespace orc
+
 // ------------------------------------------------------------------------------------------
 // C interface for the Python test harness (ctypes).
 // ------------------------------------------------------------------------------------------
@@ -1168,6 +1219,19 @@ int oracle_ir(int precision, int64_t n, const int64_t *ptr, const int64_t *idx, 
     rep[10] = static_cast<double>(r.nnz_p);
     rep[11] = r.last_inner_status;
     return r.status;
+}
+
+double oracle_spai_sample(int precision, int64_t n, const int64_t *ptr, const int64_t *idx,
+                          const double *val, double epsilon, int64_t alpha, int64_t beta,
+                          const int64_t *cols, int64_t ncols, int nthreads, int64_t *fits_out) {
+    SpaiOptions o;
+    o.epsilon = epsilon;
+    o.alpha = alpha;
+    o.beta = beta;
+    const Csr<double> a = make_csr(n, ptr, idx, val);
+    if (precision == 1)
+        return spai_sample(to_float(a), o, cols, ncols, nthreads, fits_out);
+    return spai_sample(a, o, cols, ncols, nthreads, fits_out);
 }
 
 // IR with a given preconditioner (refine_with_preconditioner, ir.cpp:138-204), binary64.

@@ -109,6 +109,7 @@ struct spai_handle_s {
     IrEngine<float, double> emix;
     IrEngine<float, float> e32;
     int engine_cap = -1;
+    KernelProfile prof;
     double spai_ms = 0;
     long long spai_launches = 0;
 
@@ -173,6 +174,7 @@ void ensure_engine(spai_handle *h, int cap) {
         h->emix.setup(h->solve, h->a64, h->a32, h->s32.p, cap, sms);
     else
         h->e32.setup(h->solve, h->a32, h->a32, h->s32.p, cap, sms);
+    h->e64.prof = h->emix.prof = h->e32.prof = &h->prof;
     h->engine_cap = cap;
 }
 
@@ -745,6 +747,32 @@ int spai_gmres(spai_handle *h, const double *rhs, double *x, double tau, int64_t
         *out_iterations = ctl.iterations;
     if (out_relative)
         *out_relative = ctl.rel;
+    return SPAI_OK;
+    API_END
+}
+
+int spai_profile(spai_handle *h, int32_t enable) {
+    API_BEGIN
+    if (!h)
+        return fail(SPAI_ERR_ARGUMENT, "spai_profile: null handle");
+    SPAI_CUDA(cudaSetDevice(h->device));
+    SPAI_CUDA(cudaStreamSynchronize(h->stream));
+    h->prof.reset();
+    h->prof.on = enable != 0;
+    return SPAI_OK;
+    API_END
+}
+
+int spai_profile_read(spai_handle *h, int32_t cls, double *ms, int64_t *launches, double *bytes) {
+    API_BEGIN
+    if (!h || cls < 0 || cls >= kClsCount)
+        return fail(SPAI_ERR_ARGUMENT, "spai_profile_read: bad arguments");
+    if (ms)
+        *ms = h->prof.ms[cls];
+    if (launches)
+        *launches = h->prof.launches[cls];
+    if (bytes)
+        *bytes = h->prof.bytes[cls];
     return SPAI_OK;
     API_END
 }

@@ -786,6 +786,63 @@ void launch_spmv(const DeviceCsr<TA> &m, VecRef<TX> x, VecRef<TY> y, const int *
     SPAI_LAUNCH("spmv_kernel");
 }
 
+// Optional per-kernel-class timing: CUDA events recorded on the solve stream around each
+// launch of the Arnoldi kernels. Launch records of speculative steps past the end of a GMRES
+// solve are discarded using the solve's iteration count.
+enum KernelClass : int { kClsSpmvA = 0, kClsSpmvP, kClsDots, kClsUpdate, kClsNormalize, kClsCount };
+struct KernelProfile {
+    bool on = false;
+    std::vector<cudaEvent_t> ev;
+    size_t next = 0;
+    struct Rec {
+        int cls, k, solve;
+        size_t e0, e1;
+        double bytes;
+    };
+    std::vector<Rec> recs;
+    std::vector<int> solve_iters;
+    double ms[kClsCount] = {0, 0, 0, 0, 0};
+    double bytes[kClsCount] = {0, 0, 0, 0, 0};
+    long long launches[kClsCount] = {0, 0, 0, 0, 0};
+    ~KernelProfile() {
+        for (auto e : ev)
+            cudaEventDestroy(e);
+    }
+    size_t mark(cudaStream_t st) {
+        if (next == ev.size()) {
+            cudaEvent_t e;
+            SPAI_CUDA(cudaEventCreate(&e));
+            ev.push_back(e);
+        }
+        SPAI_CUDA(cudaEventRecord(ev[next], st));
+        return next++;
+    }
+    void reset() {
+        next = 0;
+        recs.clear();
+        solve_iters.clear();
+        for (int c = 0; c < kClsCount; ++c) {
+            ms[c] = 0;
+            bytes[c] = 0;
+            launches[c] = 0;
+        }
+    }
+    // Accumulate the records of finished solves (all work up to the last event has completed).
+    void collect() {
+        for (const Rec &r : recs) {
+            if (r.solve >= static_cast<int>(solve_iters.size()) || r.k >= solve_iters[r.solve])
+                continue;
+            float t = 0;
+            SPAI_CUDA(cudaEventElapsedTime(&t, ev[r.e0], ev[r.e1]));
+            ms[r.cls] += t;
+            bytes[r.cls] += r.bytes;
+            launches[r.cls] += 1;
+        }
+        recs.clear();
+        next = 0;
+    }
+};
+
 // Buffers and launch sequence of one refinement solve with inner type T and outer type TO.
 template <class T, class TO> struct IrEngine {
     int n = 0, cap = 0, sms = 0;
@@ -804,6 +861,20 @@ template <class T, class TO> struct IrEngine {
     int *counters = nullptr;
     int nblk_vec = 0, nblk_dots = 0;
     long long launches = 0;
+    KernelProfile *prof = nullptr;
+    int host_k = 0, solve_index = 0;
+
+    // Launch `f` between two profile events when profiling is on.
+    template <class F> void timed(cudaStream_t st, int cls, double bytes_, F &&f) {
+        if (!prof || !prof->on) {
+            f();
+            return;
+        }
+        const size_t e0 = prof->mark(st);
+        f();
+        const size_t e1 = prof->mark(st);
+        prof->recs.push_back(KernelProfile::Rec{cls, host_k, solve_index, e0, e1, bytes_});
+    }
 
     void setup(DeviceArena &arena, const DeviceCsr<TO> &ao, const DeviceCsr<T> &ai,
                const DeviceCsr<T> &pp, int cap_, int sms_) {
@@ -856,28 +927,53 @@ template <class T, class TO> struct IrEngine {
     }
 
     // One Arnoldi step plus (when triggered) candidate verification.
+    // Algorithmic bytes of one launch (each stored element read or written once).
+    double spmv_bytes(const DeviceCsr<T> &m) const {
+        return static_cast<double>(m.nnz) * (4 + sizeof(T)) + 4.0 * (m.n + 1) +
+               2.0 * m.n * sizeof(T);
+    }
+    double vec_bytes(double vectors) const {
+        return vectors * static_cast<double>(n) * sizeof(T);
+    }
+
     void arnoldi_step(cudaStream_t st) {
-        launch_spmv<T, T, T>(*a_inner, basis_at_k(0), fixed(t), &ctl->active, sms, st);
-        launch_spmv<T, T, T>(*p, fixed(t), fixed(w), &ctl->active, sms, st);
+        const double kk = host_k;
+        timed(st, kClsSpmvA, spmv_bytes(*a_inner), [&] {
+            launch_spmv<T, T, T>(*a_inner, basis_at_k(0), fixed(t), &ctl->active, sms, st);
+        });
+        timed(st, kClsSpmvP, spmv_bytes(*p), [&] {
+            launch_spmv<T, T, T>(*p, fixed(t), fixed(w), &ctl->active, sms, st);
+        });
         const size_t dyn = sizeof(T) * static_cast<size_t>(cap + 2);
-        arnoldi_dots_kernel<T, 128><<<nblk_dots, kBlock, dyn, st>>>(n, ld, V, w, ctl, part, cap + 2,
-                                                                     h1, counters + kSlotDots);
-        SPAI_LAUNCH("arnoldi_dots_kernel");
-        arnoldi_update_kernel<T><<<nblk_vec, kBlock, 0, st>>>(n, ld, V, w, ctl, h1, npart,
-                                                               counters + kSlotUpdNorm, 0, nullptr,
-                                                               H, hld, cs, sn, g);
-        SPAI_LAUNCH("arnoldi_update_kernel(1)");
-        arnoldi_dots_kernel<T, 128><<<nblk_dots, kBlock, dyn, st>>>(n, ld, V, w, ctl, part, cap + 2,
-                                                                     h2, counters + kSlotDots);
-        SPAI_LAUNCH("arnoldi_dots_kernel(2)");
-        arnoldi_update_kernel<T><<<nblk_vec, kBlock, 0, st>>>(n, ld, V, w, ctl, h2, npart,
-                                                               counters + kSlotUpdNorm, 1, h1, H,
-                                                               hld, cs, sn, g);
-        SPAI_LAUNCH("arnoldi_update_kernel(2)");
-        normalize_kernel<T><<<nblk_vec, kBlock, 0, st>>>(n, ld, V, w, ctl);
-        SPAI_LAUNCH("normalize_kernel");
+        timed(st, kClsDots, vec_bytes(kk + 2), [&] {
+            arnoldi_dots_kernel<T, 128><<<nblk_dots, kBlock, dyn, st>>>(n, ld, V, w, ctl, part, cap + 2,
+                                                                         h1, counters + kSlotDots);
+            SPAI_LAUNCH("arnoldi_dots_kernel");
+        });
+        timed(st, kClsUpdate, vec_bytes(kk + 3), [&] {
+            arnoldi_update_kernel<T><<<nblk_vec, kBlock, 0, st>>>(n, ld, V, w, ctl, h1, npart,
+                                                                   counters + kSlotUpdNorm, 0, nullptr,
+                                                                   H, hld, cs, sn, g);
+            SPAI_LAUNCH("arnoldi_update_kernel(1)");
+        });
+        timed(st, kClsDots, vec_bytes(kk + 2), [&] {
+            arnoldi_dots_kernel<T, 128><<<nblk_dots, kBlock, dyn, st>>>(n, ld, V, w, ctl, part, cap + 2,
+                                                                         h2, counters + kSlotDots);
+            SPAI_LAUNCH("arnoldi_dots_kernel(2)");
+        });
+        timed(st, kClsUpdate, vec_bytes(kk + 3), [&] {
+            arnoldi_update_kernel<T><<<nblk_vec, kBlock, 0, st>>>(n, ld, V, w, ctl, h2, npart,
+                                                                   counters + kSlotUpdNorm, 1, h1, H,
+                                                                   hld, cs, sn, g);
+            SPAI_LAUNCH("arnoldi_update_kernel(2)");
+        });
+        timed(st, kClsNormalize, vec_bytes(2), [&] {
+            normalize_kernel<T><<<nblk_vec, kBlock, 0, st>>>(n, ld, V, w, ctl);
+            SPAI_LAUNCH("normalize_kernel");
+        });
         launches += 7;
         verify(st);
+        ++host_k;
     }
 
     void verify(cudaStream_t st) {
@@ -918,12 +1014,23 @@ template <class T, class TO> struct IrEngine {
     // Inner GMRES loop driven from the host in batches of speculative steps (steps after the
     // solve ends are no-ops gated on ctl->active).
     void gmres_loop(cudaStream_t st, bool accept_every, int *pinned) {
+        (void)accept_every;
         const int batch = 8;
+        host_k = 0;
         for (int it = 0; it < cap; it += batch) {
             for (int s = 0; s < batch && it + s < cap; ++s)
                 arnoldi_step(st);
             if (!read_flag(st, pinned, &ctl->active))
                 break;
+        }
+        if (prof && prof->on) {
+            SPAI_CUDA(cudaMemcpyAsync(pinned, &ctl->iterations, sizeof(int), cudaMemcpyDeviceToHost, st));
+            SPAI_CUDA(cudaStreamSynchronize(st));
+            prof->solve_iters.push_back(*pinned);
+            ++solve_index;
+            prof->collect();
+            prof->solve_iters.clear();
+            solve_index = 0;
         }
     }
 

@@ -96,6 +96,8 @@ SIGNATURES = {
                                              ctypes.POINTER(Report), VP]),
     "spai_adjoint": (ctypes.c_int, [VP, ctypes.c_int64, F64P, F64P, F64P, F64P, ctypes.POINTER(Options),
                                     ctypes.POINTER(Report)]),
+    "spai_profile": (ctypes.c_int, [VP, ctypes.c_int32]),
+    "spai_profile_read": (ctypes.c_int, [VP, ctypes.c_int32, F64P, I64P, F64P]),
     "spai_hypot": (ctypes.c_double, [ctypes.c_double, ctypes.c_double]),
     "spai_hypotf": (ctypes.c_float, [ctypes.c_float, ctypes.c_float]),
 }
@@ -238,6 +240,19 @@ class Handle:
         _check(lib().spai_gmres(self._h, _p(rhs, F64P), _p(x, F64P), tau, cap, ctypes.byref(st),
                                 ctypes.byref(it), ctypes.byref(rel)))
         return x, dict(status=st.value, iterations=it.value, final_relative=rel.value)
+
+    KERNEL_CLASSES = ("spmv_A", "spmv_P", "cgs_dots", "cgs_update", "normalize")
+
+    def profile(self, enable=True):
+        _check(lib().spai_profile(self._h, 1 if enable else 0))
+
+    def profile_read(self):
+        out = {}
+        for c, name in enumerate(self.KERNEL_CLASSES):
+            ms, ln, by = ctypes.c_double(), ctypes.c_int64(), ctypes.c_double()
+            _check(lib().spai_profile_read(self._h, c, ctypes.byref(ms), ctypes.byref(ln), ctypes.byref(by)))
+            out[name] = dict(ms=ms.value, launches=ln.value, bytes=by.value)
+        return out
 
     def adjoint(self, x, dldx, opts):
         x = np.asfortranarray(x, np.float64)
