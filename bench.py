@@ -280,16 +280,19 @@ def cpu_estimate(grid, fits_total, iter_counts, threads, precision="mixed", p_sy
     p_like = p_system if p_system is not None else (n, system[1], system[2], system[3] / np.max(np.abs(system[3])))
     rhs = M.equal_rhs(n)
     times = {}
-    for K in (4, 12):
+    for K in (2, 6, 14):
         t0 = time.perf_counter()
         O.gmres(system, p_like, rhs, tol=1e-30, cap=K, precision="f32" if precision != "f64" else "f64")
         times[K] = time.perf_counter() - t0
-    b = 2 * (times[12] - 3 * times[4]) / (12 * 12 - 3 * 4 * 4)
-    a = (times[4] - b * 16 / 2) / 4
+    # Least squares for t(K) = c + a K + b K^2 / 2; c (argument copies) is a per-call constant.
+    Ks = np.array(sorted(times), float)
+    A = np.stack([np.ones_like(Ks), Ks, Ks * Ks / 2], 1)
+    c, a, b = np.linalg.lstsq(A, np.array([times[int(k)] for k in Ks]), rcond=None)[0]
+    a, b = max(a, 0.0), max(b, 0.0)
     gmres_total = sum(a * K + b * K * K / 2 for K in iter_counts)
     sample = (f"oracle {precision}: SPAI fits of {len(cols)} sampled columns on {threads} threads "
-              f"({sec:.2f} s, scaled to n={n}); GMRES fixed runs of 4 and 12 steps on 1 thread fitted "
-              f"to a K + b K^2/2 and summed over the GPU run's inner iteration counts {iter_counts}")
+              f"({sec:.2f} s, scaled to n={n}); GMRES fixed runs of 2, 6 and 14 steps on 1 thread fitted "
+              f"to c + a K + b K^2/2 and summed over the GPU run's inner iteration counts {iter_counts}")
     return (spai_total + gmres_total) * 1e3, sample, {"spai_s": spai_total, "gmres_s": gmres_total}
 
 

@@ -233,12 +233,12 @@ int solve_device_impl(spai_handle *h, const double *d_b, double *d_x, const spai
         h->e64.solve(h->stream, d_b, d_x, s, h->pinned);
         rep->solve_ms = timer.stop();
         read_ctl(h, h->e64, c);
-        rep->kernel_launches = h->e64.launches;
+        rep->kernel_launches = h->e64.graph_mode ? h->e64.graph_kernels(c) : h->e64.launches;
     } else if (h->precision == SPAI_PREC_MIXED) {
         h->emix.solve(h->stream, d_b, d_x, s, h->pinned);
         rep->solve_ms = timer.stop();
         read_ctl(h, h->emix, c);
-        rep->kernel_launches = h->emix.launches;
+        rep->kernel_launches = h->emix.graph_mode ? h->emix.graph_kernels(c) : h->emix.launches;
     } else {
         // binary32 drop-in: b rounded to binary32, refinement in binary32.
         h->scratch.reset();
@@ -251,7 +251,7 @@ int solve_device_impl(spai_handle *h, const double *d_b, double *d_x, const spai
         SPAI_LAUNCH("convert_kernel");
         rep->solve_ms = timer.stop();
         read_ctl(h, h->e32, c);
-        rep->kernel_launches = h->e32.launches + 2;
+        rep->kernel_launches = (h->e32.graph_mode ? h->e32.graph_kernels(c) : h->e32.launches) + 2;
     }
     fill_from_ctl(c, rep);
     rep->nnz_p = h->precision == SPAI_PREC_F64 ? h->s64.p.nnz : h->s32.p.nnz;

@@ -32,7 +32,8 @@ struct Ctl {
     int accept_every; // binary32 drop-in acceptance (verify every step)
     int vgate;        // verification kernels of this step run
     int pending;      // an update x_new = x + d awaits its diagnostics
-    int pad[1];
+    int guard;        // Arnoldi steps run in this solve (bounds every device-side loop)
+    int verifications; // candidate checks run in this solve
     double be, cbe, rinf, xinf, bscale, anorm_inf, binf;
     double inner_scale; // power of two applied to the correction right-hand side
     double tol_inner;

@@ -416,6 +416,7 @@ __global__ void decide_kernel(Ctl *ctl, const T *orig, const T *relnum) {
     const int accept_every = ctl->accept_every;
     const bool verified = ctl->vgate != 0;
     ctl->vgate = 0;
+    ctl->verifications += verified ? 1 : 0;
     if (verified) {
         const double rel = static_cast<double>(*relnum) / ctl->den;
         ctl->rel = rel;
@@ -449,8 +450,22 @@ __global__ void decide_kernel(Ctl *ctl, const T *orig, const T *relnum) {
         ctl->active = 0;
         return;
     }
+    // Device-side loop bound: at most cap steps per inner solve and (outer_cap + 1) solves.
+    if (++ctl->guard > (ctl->cap + 1) * (ctl->outer_cap + 2)) {
+        ctl->status = 8;
+        ctl->active = 0;
+        ctl->outer_active = 0;
+        ctl->ir_status = 6;
+        return;
+    }
     ctl->k += 1;
     ctl->triggered = 0;
+}
+
+// Copies a device flag into a graph conditional handle (loop / branch condition).
+__global__ void set_cond_kernel(cudaGraphConditionalHandle h, const int *flag) {
+    if (threadIdx.x == 0)
+        cudaGraphSetConditional(h, *flag ? 1u : 0u);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -863,6 +878,112 @@ template <class T, class TO> struct IrEngine {
     long long launches = 0;
     KernelProfile *prof = nullptr;
     int host_k = 0, solve_index = 0;
+    TO *bbuf = nullptr, *xbuf = nullptr; // fixed graph-side copies of b and x
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    bool graph_f32_accept = false;
+    bool graph_mode = false;
+
+    // Kernel nodes executed by the last graph solve, from the device loop counters: 4 init
+    // nodes; per GMRES solve 8 start nodes and 6 update/residual nodes; per Arnoldi step 7 passes,
+    // 2 condition sets and the decision; per candidate verification 6.
+    long long graph_kernels(const Ctl &c) const {
+        const long long steps = static_cast<long long>(c.guard) + c.inner_attempts;
+        return 4 + 14LL * c.inner_attempts + 10LL * steps + 6LL * c.verifications;
+    }
+
+    ~IrEngine() {
+        release_graph();
+    }
+    void release_graph() {
+        if (exec)
+            cudaGraphExecDestroy(exec);
+        if (graph)
+            cudaGraphDestroy(graph);
+        exec = nullptr;
+        graph = nullptr;
+    }
+
+    // Capture the launches of `f` into graph g after `deps`; returns the new leaf set.
+    template <class F>
+    std::vector<cudaGraphNode_t> capture_into(cudaStream_t st, cudaGraph_t g,
+                                              const std::vector<cudaGraphNode_t> &deps, F &&f) {
+        SPAI_CUDA(cudaStreamBeginCaptureToGraph(st, g, deps.empty() ? nullptr : deps.data(), nullptr,
+                                                deps.size(), cudaStreamCaptureModeRelaxed));
+        f();
+        cudaStreamCaptureStatus cs;
+        const cudaGraphNode_t *d = nullptr;
+        size_t nd = 0;
+        SPAI_CUDA(cudaStreamGetCaptureInfo(st, &cs, nullptr, nullptr, &d, nullptr, &nd));
+        std::vector<cudaGraphNode_t> out(d, d + nd);
+        cudaGraph_t tmp = nullptr;
+        SPAI_CUDA(cudaStreamEndCapture(st, &tmp));
+        return out;
+    }
+    cudaGraphNode_t add_conditional(cudaGraph_t g, const std::vector<cudaGraphNode_t> &deps,
+                                    cudaGraphConditionalHandle h, cudaGraphConditionalNodeType type,
+                                    cudaGraph_t *body) {
+        cudaGraphNodeParams p{};
+        p.type = cudaGraphNodeTypeConditional;
+        p.conditional.handle = h;
+        p.conditional.type = type;
+        p.conditional.size = 1;
+        cudaGraphNode_t node;
+        SPAI_CUDA(cudaGraphAddNode(&node, g, deps.empty() ? nullptr : deps.data(), nullptr, deps.size(), &p));
+        *body = p.conditional.phGraph_out[0];
+        return node;
+    }
+
+    // The whole refinement solve as one graph: init, then WHILE(outer) { rhs, GMRES start,
+    // WHILE(inner) { Arnoldi step, IF(verify) { candidate check }, decide }, update, residual }.
+    void build_graph(cudaStream_t st, bool accept_every) {
+        release_graph();
+        SPAI_CUDA(cudaGraphCreate(&graph, 0));
+        cudaGraphConditionalHandle h_outer;
+        SPAI_CUDA(cudaGraphConditionalHandleCreate(&h_outer, graph, 0, 0));
+        auto d0 = capture_into(st, graph, {}, [&] {
+            norms_inf_kernel<TO><<<nblk_vec, kBlock, 0, st>>>(n, a_outer->rp, a_outer->val, bbuf, dpart,
+                                                              ctl, counters + kSlotMisc);
+            ir_x0_kernel<T, TO><<<nblk_vec, kBlock, 0, st>>>(n, p->rp, p->ci, p->val, bbuf, xbuf);
+            residual(st, bbuf, xbuf);
+            set_cond_kernel<<<1, 32, 0, st>>>(h_outer, &ctl->outer_active);
+        });
+        cudaGraph_t body_outer;
+        const auto n_outer = add_conditional(graph, d0, h_outer, cudaGraphCondTypeWhile, &body_outer);
+        (void)n_outer;
+        cudaGraphConditionalHandle h_inner;
+        SPAI_CUDA(cudaGraphConditionalHandleCreate(&h_inner, body_outer, 0, 0));
+        auto d1 = capture_into(st, body_outer, {}, [&] {
+            make_rhs_kernel<TO, T><<<nblk_vec, kBlock, 0, st>>>(n, r, rhs, ctl);
+            gmres_start(st, accept_every);
+            set_cond_kernel<<<1, 32, 0, st>>>(h_inner, &ctl->active);
+        });
+        cudaGraph_t body_inner;
+        const auto n_inner = add_conditional(body_outer, d1, h_inner, cudaGraphCondTypeWhile, &body_inner);
+        cudaGraphConditionalHandle h_verify;
+        SPAI_CUDA(cudaGraphConditionalHandleCreate(&h_verify, body_inner, 0, 0));
+        auto e1 = capture_into(st, body_inner, {}, [&] {
+            arnoldi_passes(st);
+            set_cond_kernel<<<1, 32, 0, st>>>(h_verify, &ctl->vgate);
+        });
+        cudaGraph_t body_verify;
+        const auto n_verify = add_conditional(body_inner, e1, h_verify, cudaGraphCondTypeIf, &body_verify);
+        capture_into(st, body_verify, {}, [&] { verify_checks(st); });
+        capture_into(st, body_inner, {n_verify}, [&] {
+            decide_kernel<T><<<1, 32, 0, st>>>(ctl, scal + 0, scal + 1);
+            set_cond_kernel<<<1, 32, 0, st>>>(h_inner, &ctl->active);
+        });
+        capture_into(st, body_outer, {n_inner}, [&] {
+            ir_after_inner_kernel<<<1, 32, 0, st>>>(ctl);
+            ir_update_kernel<TO, T><<<nblk_vec, kBlock, 0, st>>>(n, xbuf, xn, cand, ctl);
+            ir_after_update_kernel<<<1, 32, 0, st>>>(ctl);
+            residual(st, bbuf, xn);
+            ir_commit_kernel<TO><<<nblk_vec, kBlock, 0, st>>>(n, xbuf, xn, ctl);
+            set_cond_kernel<<<1, 32, 0, st>>>(h_outer, &ctl->outer_active);
+        });
+        SPAI_CUDA(cudaGraphInstantiate(&exec, graph, 0));
+        graph_f32_accept = accept_every;
+    }
 
     // Launch `f` between two profile events when profiling is on.
     template <class F> void timed(cudaStream_t st, int cls, double bytes_, F &&f) {
@@ -899,6 +1020,9 @@ template <class T, class TO> struct IrEngine {
         pax = arena.alloc<T>(ld);
         r = arena.alloc<TO>(ld);
         xn = arena.alloc<TO>(ld);
+        bbuf = arena.alloc<TO>(ld);
+        xbuf = arena.alloc<TO>(ld);
+        release_graph();
         H = arena.alloc<T>(static_cast<size_t>(hld) * (cap + 1));
         cs = arena.alloc<T>(cap + 1);
         sn = arena.alloc<T>(cap + 1);
@@ -937,6 +1061,12 @@ template <class T, class TO> struct IrEngine {
     }
 
     void arnoldi_step(cudaStream_t st) {
+        arnoldi_passes(st);
+        verify(st);
+        ++host_k;
+    }
+
+    void arnoldi_passes(cudaStream_t st) {
         const double kk = host_k;
         timed(st, kClsSpmvA, spmv_bytes(*a_inner), [&] {
             launch_spmv<T, T, T>(*a_inner, basis_at_k(0), fixed(t), &ctl->active, sms, st);
@@ -972,11 +1102,16 @@ template <class T, class TO> struct IrEngine {
             SPAI_LAUNCH("normalize_kernel");
         });
         launches += 7;
-        verify(st);
-        ++host_k;
     }
 
     void verify(cudaStream_t st) {
+        verify_checks(st);
+        decide_kernel<T><<<1, 32, 0, st>>>(ctl, scal + 0, scal + 1);
+        SPAI_LAUNCH("decide_kernel");
+        ++launches;
+    }
+
+    void verify_checks(cudaStream_t st) {
         solve_y_kernel<T><<<1, 32, 0, st>>>(ctl, H, hld, g, y);
         SPAI_LAUNCH("solve_y_kernel");
         form_candidate_kernel<T><<<nblk_vec, kBlock, 0, st>>>(n, ld, V, y, cand, ctl);
@@ -986,9 +1121,7 @@ template <class T, class TO> struct IrEngine {
         norm(st, fixed(rhs), ax, scal + 0, kSlotNormA, g2);
         launch_spmv<T, T, T>(*p, fixed(ax), fixed(pax), g2, sms, st);
         norm(st, fixed(pb), pax, scal + 1, kSlotNormB, g2);
-        decide_kernel<T><<<1, 32, 0, st>>>(ctl, scal + 0, scal + 1);
-        SPAI_LAUNCH("decide_kernel");
-        launches += 5;
+        launches += 4;
     }
 
     // GMRES start for the current rhs (x0 = 0): ||rhs||, Pb, ||Pb||, v0 = Pb/||Pb||.
@@ -1056,6 +1189,7 @@ template <class T, class TO> struct IrEngine {
     // Full refinement solve; b, x are device vectors in TO.
     void solve(cudaStream_t st, const TO *b, TO *x, const SolveSettings &s, int *pinned) {
         launches = 0;
+        graph_mode = false;
         Ctl h{};
         h.cap = cap;
         h.outer_cap = s.outer_cap;
@@ -1070,6 +1204,15 @@ template <class T, class TO> struct IrEngine {
         h.accept_every = s.accept_every ? 1 : 0;
         SPAI_CUDA(cudaMemcpyAsync(ctl, &h, sizeof(Ctl), cudaMemcpyHostToDevice, st));
         SPAI_CUDA(cudaMemsetAsync(counters, 0, 16 * sizeof(int), st));
+        if (s.use_graph && !(prof && prof->on)) {
+            if (!exec || graph_f32_accept != s.accept_every)
+                build_graph(st, s.accept_every);
+            SPAI_CUDA(cudaMemcpyAsync(bbuf, b, sizeof(TO) * n, cudaMemcpyDeviceToDevice, st));
+            SPAI_CUDA(cudaGraphLaunch(exec, st));
+            SPAI_CUDA(cudaMemcpyAsync(x, xbuf, sizeof(TO) * n, cudaMemcpyDeviceToDevice, st));
+            graph_mode = true;
+            return;
+        }
         norms_inf_kernel<TO><<<nblk_vec, kBlock, 0, st>>>(n, a_outer->rp, a_outer->val, b, dpart,
                                                           ctl, counters + kSlotMisc);
         SPAI_LAUNCH("norms_inf_kernel");
