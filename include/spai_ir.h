@@ -201,6 +201,22 @@ int spai_adjoint(spai_handle *h, int64_t nrhs, const double *x, const double *dL
 int spai_profile(spai_handle *h, int32_t enable);
 int spai_profile_read(spai_handle *h, int32_t cls, double *ms, int64_t *launches, double *bytes);
 
+/* Backward error of a given x with no device allocation (no counterpart in the reference).
+ * For callers that cannot call cudaMalloc where they need this check: applications whose device
+ * memory is owned by their own pool/caching allocator, and latency-critical loops that cannot
+ * afford an allocation's implicit synchronisation. d_b, d_x: binary64 device vectors of the
+ * handle's n; d_out: device array of 3 doubles receiving {normwise backward error,
+ * componentwise backward error, ||b - A x||_inf}. The handle must hold A in binary64
+ * (SPAI_PREC_F64 or SPAI_PREC_MIXED). Scratch (the residual and per-block partials) is a fixed
+ * file-scope device array of 4 MiB + 33 KiB that every GPU loading the library keeps until exit;
+ * systems with n > 524288 rows are rejected with SPAI_ERR_ARGUMENT. The first call on a device
+ * looks up that array's address (once per device); make this first call before any stream
+ * capture. All calls share the array and it keeps the last call's contents; calls that overlap
+ * on the GPU race. stream: cudaStream_t to launch on, NULL = the handle's stream. The call is
+ * asynchronous; synchronise the stream before reading d_out. */
+int spai_backward_error_noalloc(spai_handle *h, const double *d_b, const double *d_x,
+                                double *d_out, void *stream);
+
 /* Host builds of the device hypot used by the SPAI fits (parity tests). */
 double spai_hypot(double a, double b);
 float spai_hypotf(float a, float b);

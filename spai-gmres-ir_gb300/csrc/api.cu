@@ -126,6 +126,17 @@ struct spai_handle_s {
     }
 };
 
+void handle_view(spai_handle_s *h, spai::HandleView &v) {
+    v.precision = h->precision;
+    v.device = h->device;
+    v.sms = h->sms;
+    v.stream = h->stream;
+    v.a64 = &h->a64;
+}
+int spai_api_fail(int code, const std::string &msg) {
+    return spai_api::fail(code, msg);
+}
+
 namespace spai_api {
 
 void fill_defaults(spai_options *o, int32_t precision) {

@@ -6,6 +6,7 @@
 
 #include <cstddef>
 #include <cstdint>
+#include <string>
 #include <vector>
 
 namespace spai {
@@ -95,5 +96,20 @@ template <class T> struct SpaiBuilder {
 };
 
 template <class T> void score_kat(T rsq, T dot, T den, double *out);
+
+// Read-only view of a handle's resident matrix for entry points outside the API unit.
+struct HandleView {
+    int precision = 0, device = 0, sms = 0;
+    cudaStream_t stream = nullptr;
+    const DeviceCsr<double> *a64 = nullptr;
+};
+
+} // namespace spai
+
+struct spai_handle_s;
+void handle_view(spai_handle_s *h, spai::HandleView &v);
+int spai_api_fail(int code, const std::string &msg);
+
+namespace spai {
 
 } // namespace spai

@@ -98,6 +98,7 @@ SIGNATURES = {
                                     ctypes.POINTER(Report)]),
     "spai_profile": (ctypes.c_int, [VP, ctypes.c_int32]),
     "spai_profile_read": (ctypes.c_int, [VP, ctypes.c_int32, F64P, I64P, F64P]),
+    "spai_backward_error_noalloc": (ctypes.c_int, [VP, VP, VP, VP, VP]),
     "spai_hypot": (ctypes.c_double, [ctypes.c_double, ctypes.c_double]),
     "spai_hypotf": (ctypes.c_float, [ctypes.c_float, ctypes.c_float]),
 }
@@ -240,6 +241,10 @@ class Handle:
         _check(lib().spai_gmres(self._h, _p(rhs, F64P), _p(x, F64P), tau, cap, ctypes.byref(st),
                                 ctypes.byref(it), ctypes.byref(rel)))
         return x, dict(status=st.value, iterations=it.value, final_relative=rel.value)
+
+    def backward_error_noalloc(self, d_b, d_x, d_out, stream=None):
+        """Allocation-free backward error of device vector x (see spai_backward_error_noalloc)."""
+        _check(lib().spai_backward_error_noalloc(self._h, VP(d_b), VP(d_x), VP(d_out), stream))
 
     KERNEL_CLASSES = ("spmv_A", "spmv_P", "cgs_dots", "cgs_update", "normalize")
 

@@ -20,6 +20,7 @@ COMMON = ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I" +
 UNITS = {
     "spai_build.o": ("spai_build.cu", ["--fmad=false"]),
     "api.o": ("api.cu", []),
+    "noalloc.o": ("noalloc.cu", []),
 }
 HEADERS = ["common.cuh", "exact_math.cuh", "spai_internal.hpp", "krylov.cuh", "krylov_kernels.cuh",
            "mm_io.hpp"]
