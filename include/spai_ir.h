@@ -82,7 +82,10 @@ enum { SPAI_PREC_F64 = 0, SPAI_PREC_F32 = 1, SPAI_PREC_MIXED = 2 };
 
 /* Option flags. */
 enum {
-    SPAI_FLAG_NO_GRAPH = 1 /* run the refinement loop with host launches instead of one graph */
+    SPAI_FLAG_NO_GRAPH = 1,  /* run the refinement loop with host launches instead of one graph */
+    SPAI_FLAG_FAST_SPAI = 2  /* build the SPAI with group-parallel norms, a parallel mean and hashed
+                                candidate sets instead of the reference's sequential arithmetic
+                                (patterns may differ on near-tied scores; not bit-reproducible) */
 };
 
 /* Canonical CSR on the host (row_offsets[n+1], sorted col_indices[nnz], no stored zeros), the
@@ -194,8 +197,8 @@ int spai_adjoint(spai_handle *h, int64_t nrhs, const double *x, const double *dL
                  double *dLdb, double *dLdA_values, const spai_options *opt, spai_report *rep);
 
 /* Per-kernel-class timing of refinement solves (CUDA events on the handle's stream around each
- * launch). Classes: 0 SpMV with A, 1 SpMV with P, 2 Gram-Schmidt dot pass, 3 Gram-Schmidt update
- * pass, 4 normalisation. enable != 0 resets and starts recording; read returns the accumulated
+ * launch). Classes: 0 SpMV with A (basis vector gathered), 1 SpMV with P, 2 Gram-Schmidt pass 1
+ * (dots), 3 pass 2 (update + dots), 4 pass 3 (reorthogonalisation, only when it runs). enable != 0 resets and starts recording; read returns the accumulated
  * device milliseconds, launch count and algorithmic bytes of one class. No reference
  * counterpart (the reference only kept host wall-clock telemetry, src/cuda_spai.cu:19-38). */
 int spai_profile(spai_handle *h, int32_t enable);

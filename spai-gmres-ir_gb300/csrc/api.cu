@@ -5,6 +5,7 @@
 
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <type_traits>
@@ -340,8 +341,12 @@ int spai_create(const spai_csr *a, int32_t precision, int device, void *stream, 
     }
     SPAI_CUDA(cudaMallocHost(&h->pinned, 64));
     const int n = h->n, nnz = h->nnz;
+    int max_row = 0;
+    for (int64_t r = 0; r < a->n; ++r)
+        max_row = std::max<int>(max_row, static_cast<int>(a->row_offsets[r + 1] - a->row_offsets[r]));
     h->a64.n = n;
     h->a64.nnz = nnz;
+    h->a64.max_row = max_row;
     h->a64.rp = h->mat.alloc<int>(n + 1);
     h->a64.ci = h->mat.alloc<int>(nnz);
     h->a64.val = h->mat.alloc<double>(nnz);
@@ -359,6 +364,7 @@ int spai_create(const spai_csr *a, int32_t precision, int device, void *stream, 
     if (precision != SPAI_PREC_F64) {
         h->a32.n = n;
         h->a32.nnz = nnz;
+        h->a32.max_row = max_row;
         h->a32.rp = h->a64.rp;
         h->a32.ci = h->a64.ci;
         h->a32.val = h->mat.alloc<float>(nnz);
@@ -394,7 +400,15 @@ int spai_build(spai_handle *h, const spai_options *opt, spai_report *rep) {
     h->engine_cap = -1;
     h->build.reset();
     SpaiParams prm;
+    // Tuning overrides (group width, per-group workspace) for profiling sweeps.
+    if (const char *e = std::getenv("SPAI_GROUP_LANES"))
+        prm.group_lanes = std::atoi(e);
+    if (const char *e = std::getenv("SPAI_WS_BYTES"))
+        prm.ws_bytes_per_warp = std::atoi(e);
     prm.epsilon = opt->epsilon;
+    // Every form follows the reference's sequential arithmetic bit for bit by default; the
+    // group-parallel variant (parallel norms and mean, hashed candidate sets) is opt-in.
+    prm.fast = (opt->flags & SPAI_FLAG_FAST_SPAI) != 0;
     prm.alpha = opt->alpha;
     prm.beta = static_cast<int>(std::min<int64_t>(opt->beta, INT_MAX));
     if (opt->alpha < 0 || opt->beta < 0)

@@ -1,0 +1,470 @@
+// Gram-Schmidt passes over a tile-major Krylov basis.
+//
+// Layout: the basis is stored in row tiles of R rows; tile t holds the R-row segments of all
+// cap+1 vectors contiguously (segment j of tile t at base + (t*(cap+1) + j)*R). A block that owns
+// tile t therefore streams one contiguous region of (k+1)*R*s bytes per pass, staged into shared
+// memory with cp.async in chunks of up to JB segments.
+//
+// Vectors are stored unnormalised: v_j = s_j W_j with the scale s_j kept on the device, so the
+// Arnoldi step needs no normalisation pass (the next SpMV and every later pass apply s_j).
+//
+// One Arnoldi step (classical Gram-Schmidt with DGKS-criterion reorthogonalisation):
+//   pass 1: d_j = W_j^T w, ||w||                           (reads V once)
+//   pass 2: w' = w - sum_j h1_j v_j, written as W_{k+1}; d2_j = W_j^T w', ||w'||  (reads V once)
+//   pass 3 (only if ||w'|| < eta ||w||): w'' = w' - sum_j h2_j v_j, ||w''||       (reads V once)
+// The last block of the finishing pass forms the Hessenberg column (h1 [+ h2], ||w'|| or ||w''||),
+// applies the Givens rotations and sets the acceptance flags, exactly as the single-pass
+// version did. Reductions are deterministic (fixed tile assignment, fixed trees).
+#pragma once
+#include "common.cuh"
+#include "exact_math.cuh"
+#include "krylov.cuh"
+
+namespace spai {
+
+template <class T> struct TileGeom;
+template <> struct TileGeom<float> {
+    static constexpr int R = 128; // 512-byte segments
+};
+template <> struct TileGeom<double> {
+    static constexpr int R = 64; // 512-byte segments
+};
+constexpr int kCgsThreads = 256;
+constexpr int kCgsJB = 192; // segments per shared-memory chunk (96 KiB)
+
+template <class T> struct Basis {
+    T *base;
+    int cap1;     // cap + 1 segments per tile
+    int ntiles;
+    const T *scale; // s_j, j <= cap
+    __device__ __forceinline__ T *seg(int tile, int j) const {
+        return base + (static_cast<long long>(tile) * cap1 + j) * TileGeom<T>::R;
+    }
+    __device__ __forceinline__ T &at(int i, int j) const {
+        constexpr int R = TileGeom<T>::R;
+        return seg(i / R, j)[i % R];
+    }
+};
+
+// Power-of-two scaled sum of squares: value = s * 2^(2e); combine is exact rescaling.
+template <class T> struct Ssq {
+    int e;
+    T s;
+};
+template <class T> __device__ __forceinline__ Ssq<T> ssq_combine(Ssq<T> a, Ssq<T> b) {
+    if (a.e == INT_MIN)
+        return b;
+    if (b.e == INT_MIN)
+        return a;
+    const int E = max(a.e, b.e);
+    return Ssq<T>{E, ldexp(a.s, 2 * (a.e - E)) + ldexp(b.s, 2 * (b.e - E))};
+}
+template <class T> __device__ __forceinline__ T ssq_value(Ssq<T> a) {
+    return a.e == INT_MIN ? T(0) : ldexp(sqrt(a.s), a.e);
+}
+
+struct CgsScratch {
+    void *dots;     // [gridDim][cap+2] of T
+    void *norms;    // [gridDim] of Ssq<T>
+    int *counter;   // last-block ticket
+};
+
+template <class T> struct CgsArgs {
+    int n;
+    Basis<T> V;
+    const T *w;         // plain vector P A v_k (pass 1 and 2 input)
+    T *h1, *h2, *H, *cs, *sn, *g, *s;  // s: writable scales (s_{k+1} set by the finishing pass)
+    int hld;
+    Ctl *ctl;
+    CgsScratch scr;
+    int always_reorth;
+};
+
+// cp.async 16-byte copies global -> shared (no spin-wait; completion via wait_group).
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
+    const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+    asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
+}
+
+// Load segments [j0, j1) of tile t into buf (rows of a partial last tile are copied too: the
+// basis storage is padded to whole tiles and kept zero beyond n).
+template <class T>
+__device__ __forceinline__ void load_chunk(const Basis<T> &V, int t, int j0, int j1, T *buf) {
+    constexpr int R = TileGeom<T>::R;
+    const char *src = reinterpret_cast<const char *>(V.seg(t, j0));
+    char *dst = reinterpret_cast<char *>(buf);
+    const int bytes = (j1 - j0) * R * static_cast<int>(sizeof(T));
+    for (int o = threadIdx.x * 16; o < bytes; o += blockDim.x * 16)
+        cp_async16(dst + o, src + o);
+    cp_async_wait_all();
+    __syncthreads();
+}
+
+template <class T> __device__ T block_sum(T v, T *red) {
+    for (int o = 16; o > 0; o >>= 1)
+        v += __shfl_xor_sync(0xffffffffu, v, o);
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0)
+        red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    T r = 0;
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i)
+        r += red[i];
+    __syncthreads();
+    return r; // every thread, same order
+}
+template <class T> __device__ T block_max(T v, T *red) {
+    for (int o = 16; o > 0; o >>= 1)
+        v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0)
+        red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    T r = 0;
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i)
+        r = fmax(r, red[i]);
+    __syncthreads();
+    return r;
+}
+
+// Givens update of Hessenberg column k (src/gmres.cpp:191-214) and the acceptance triggers.
+// Runs in one thread after the column col[0..k+1] has been written.
+template <class T> __device__ void finish_column(Ctl *ctl, T *H, int hld, T *cs, T *sn, T *g, T *s,
+                                                 T hnext, bool nonfinite) {
+    const int k = ctl->k;
+    T *col = H + static_cast<long long>(k) * hld;
+    col[k + 1] = hnext;
+    nonfinite |= !isfinite(hnext);
+    ctl->hnext = static_cast<double>(hnext);
+    ctl->breakdown = hnext == T(0);
+    s[k + 1] = hnext == T(0) ? T(0) : T(1) / hnext;
+    for (int r = 0; r < k; ++r) {
+        const T up = col[r], lo = col[r + 1];
+        col[r] = cs[r] * up + sn[r] * lo;
+        col[r + 1] = -sn[r] * up + cs[r] * lo;
+    }
+    const T upper = col[k];
+    const T radius = cr_hypot<T>(upper, col[k + 1]);
+    ctl->iterations = k + 1;
+    if (nonfinite || !isfinite(radius)) {
+        ctl->status = 8;
+        ctl->active = 0;
+        ctl->triggered = 0;
+        ctl->vgate = 0;
+        return;
+    }
+    if (radius == T(0)) {
+        ctl->triggered = 2; // verify the previously defined candidate (gmres.cpp:218-234)
+        ctl->vgate = 1;
+        return;
+    }
+    cs[k] = upper / radius;
+    sn[k] = col[k + 1] / radius;
+    col[k] = radius;
+    col[k + 1] = 0;
+    const T old = g[k];
+    g[k] = cs[k] * old;
+    g[k + 1] = -sn[k] * old;
+    const T est = fabs(g[k + 1]) / static_cast<T>(ctl->den);
+    ctl->est = static_cast<double>(est);
+    const bool trig = ctl->breakdown || est <= static_cast<T>(ctl->tol_inner) || k + 1 == ctl->cap;
+    ctl->triggered = trig ? 1 : 0;
+    ctl->vgate = (trig || ctl->accept_every) ? 1 : 0;
+}
+
+// One Gram-Schmidt pass (MODE 1, 2 or 3, see the file comment). Grid: persistent over tiles.
+template <class T, int MODE>
+__global__ void __launch_bounds__(kCgsThreads) cgs_pass_kernel(CgsArgs<T> a) {
+    constexpr int R = TileGeom<T>::R;
+    Ctl *ctl = a.ctl;
+    if (!ctl->active)
+        return;
+    if (MODE == 3 && !ctl->reorth)
+        return;
+    extern __shared__ __align__(16) unsigned char dyn[];
+    T *buf = reinterpret_cast<T *>(dyn);            // [kCgsJB * R]
+    T *wt = buf + kCgsJB * R;                        // [R]
+    T *acc = wt + R;                                 // [cap + 2] dot accumulators
+    T *cf = acc + (ctl->cap + 2);                    // [cap + 2] update coefficients h_j s_j
+    constexpr int NP = kCgsThreads / R; // threads per row in the update
+    __shared__ T red[kCgsThreads / 32];
+    __shared__ T part_sum[NP][R];
+    const int k = ctl->k;
+    const int kk = k + 1; // segments 0..k
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const T *coef = MODE == 2 ? a.h1 : a.h2; // h_j (coefficient h_j s_j applied below)
+    for (int j = threadIdx.x; j < kk; j += blockDim.x) {
+        acc[j] = 0;
+        if (MODE >= 2)
+            cf[j] = coef[j] * a.V.scale[j];
+    }
+    // Per-thread power-of-two scaled sum of squares of the current vector (no block syncs):
+    // value = ts * 2^(2 te); rescaling by powers of two is exact.
+    int te = INT_MIN;
+    T ts = 0;
+    bool bad = false;
+    for (int t = blockIdx.x; t < a.V.ntiles; t += gridDim.x) {
+        const int row0 = t * R;
+        const int rows = min(R, a.n - row0);
+        __syncthreads();
+        // Current vector segment.
+        if (threadIdx.x < R) {
+            T v = 0;
+            if (threadIdx.x < rows)
+                v = MODE == 3 ? a.V.seg(t, kk)[threadIdx.x] : a.w[row0 + threadIdx.x];
+            wt[threadIdx.x] = v;
+        }
+        __syncthreads();
+        bool resident = false; // the single chunk [0, kk) is still in buf
+        if (MODE >= 2) {
+            // wt -= sum_j (h_j s_j) W_j over all chunks; NP threads per row split each chunk
+            // into contiguous sub-ranges, combined in fixed order.
+            const int row = threadIdx.x % R, part = threadIdx.x / R;
+            T accr = 0;
+            for (int j0 = 0; j0 < kk; j0 += kCgsJB) {
+                const int j1 = min(kk, j0 + kCgsJB);
+                load_chunk(a.V, t, j0, j1, buf);
+                const int len = j1 - j0, per = (len + NP - 1) / NP;
+                const int ja = j0 + min(len, part * per), jb = j0 + min(len, (part + 1) * per);
+#pragma unroll 4
+                for (int j = ja; j < jb; ++j)
+                    accr += cf[j] * buf[(j - j0) * R + row];
+                resident = (j0 == 0 && j1 == kk);
+                __syncthreads();
+            }
+            part_sum[part][row] = accr;
+            __syncthreads();
+            if (part == 0) {
+                T tot = 0;
+                for (int q = 0; q < NP; ++q)
+                    tot += part_sum[q][row];
+                const T nv = row < rows ? wt[row] - tot : T(0);
+                wt[row] = nv;
+                a.V.seg(t, kk)[row] = nv; // W_{k+1} (pad rows stay zero)
+            }
+            __syncthreads();
+        }
+        if (MODE <= 2) {
+            // d_j += W_j^T wt over this tile; one warp per basis vector.
+            for (int j0 = 0; j0 < kk; j0 += kCgsJB) {
+                const int j1 = min(kk, j0 + kCgsJB);
+                if (!resident)
+                    load_chunk(a.V, t, j0, j1, buf);
+                for (int j = j0 + warp; j < j1; j += nw) {
+                    const T *sg = buf + (j - j0) * R;
+                    T sdot = 0;
+#pragma unroll
+                    for (int i = lane; i < R; i += 32)
+                        sdot += sg[i] * wt[i];
+                    for (int o = 16; o > 0; o >>= 1)
+                        sdot += __shfl_xor_sync(0xffffffffu, sdot, o);
+                    if (lane == 0)
+                        acc[j] += sdot;
+                }
+                __syncthreads();
+            }
+        }
+        if (threadIdx.x < R) {
+            const T v = wt[threadIdx.x];
+            bad |= !isfinite(v);
+            if (v != T(0) && isfinite(v)) {
+                const int ev = ilogb(v);
+                if (ev > te) {
+                    if (te != INT_MIN)
+                        ts = ldexp(ts, 2 * (te - ev));
+                    te = ev;
+                }
+                const T sv = ldexp(v, -te);
+                ts += sv * sv;
+            }
+        }
+    }
+    // Block combine of the per-thread (te, ts) pairs: common exponent, then a fixed-order sum.
+    int be = te;
+    for (int o = 16; o > 0; o >>= 1)
+        be = max(be, __shfl_xor_sync(0xffffffffu, be, o));
+    __shared__ int be_sh[kCgsThreads / 32];
+    if (lane == 0)
+        be_sh[warp] = be;
+    __syncthreads();
+    be = INT_MIN;
+    for (int i = 0; i < nw; ++i)
+        be = max(be, be_sh[i]);
+    const T scaled = (te == INT_MIN || be == INT_MIN) ? T(0) : ldexp(ts, 2 * (te - be));
+    const T bsum = block_sum(scaled, red);
+    const Ssq<T> nrm{be, bsum};
+    // Publish block partials.
+    T *dots = static_cast<T *>(a.scr.dots);
+    Ssq<T> *norms = static_cast<Ssq<T> *>(a.scr.norms);
+    const int ps = ctl->cap + 2;
+    __syncthreads();
+    if (MODE <= 2)
+        for (int j = threadIdx.x; j < kk; j += blockDim.x)
+            dots[static_cast<long long>(blockIdx.x) * ps + j] = acc[j];
+    bad = __syncthreads_or(bad);
+    if (threadIdx.x == 0)
+        norms[blockIdx.x] = bad ? Ssq<T>{INT_MAX, T(NAN)} : nrm;
+    // Last-block ticket.
+    __shared__ int is_last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const int tk = atomicAdd(a.scr.counter, 1);
+        is_last = tk == static_cast<int>(gridDim.x) - 1;
+        if (is_last)
+            *a.scr.counter = 0;
+    }
+    __syncthreads();
+    if (!is_last)
+        return;
+    __threadfence();
+    const int nb = gridDim.x;
+    // Dots: one warp per j, lanes over blocks, fixed tree.
+    T *hout = MODE == 1 ? a.h1 : a.h2;
+    if (MODE <= 2)
+        for (int j = warp; j < kk; j += nw) {
+            T sdot = 0;
+            for (int b = lane; b < nb; b += 32)
+                sdot += dots[static_cast<long long>(b) * ps + j];
+            for (int o = 16; o > 0; o >>= 1)
+                sdot += __shfl_xor_sync(0xffffffffu, sdot, o);
+            if (lane == 0)
+                hout[j] = sdot * a.V.scale[j]; // h_j = s_j W_j^T w
+        }
+    // Norm: parallel max of exponents, then rescaled sum (fixed tree).
+    __shared__ int emax_sh;
+    int emax = INT_MIN;
+    bool nb_bad = false;
+    for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+        emax = max(emax, norms[b].e == INT_MAX ? INT_MIN : norms[b].e);
+        nb_bad |= norms[b].e == INT_MAX;
+    }
+    for (int o = 16; o > 0; o >>= 1)
+        emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, o));
+    if (threadIdx.x == 0)
+        emax_sh = INT_MIN;
+    __syncthreads();
+    if (lane == 0)
+        atomicMax(&emax_sh, emax);
+    nb_bad = __syncthreads_or(nb_bad);
+    const int E = emax_sh;
+    T part_s = 0;
+    if (E != INT_MIN)
+        for (int b = threadIdx.x; b < nb; b += blockDim.x)
+            if (norms[b].e != INT_MIN && norms[b].e != INT_MAX)
+                part_s += ldexp(norms[b].s, 2 * (norms[b].e - E));
+    const T S = block_sum(part_s, red);
+    __syncthreads();
+    if (threadIdx.x != 0)
+        return;
+    const T nrm_all = nb_bad ? T(NAN) : (E == INT_MIN ? T(0) : ldexp(sqrt(S), E));
+    const int kcol = k;
+    T *col = a.H + static_cast<long long>(kcol) * a.hld;
+    if (MODE == 1) {
+        ctl->wnorm = static_cast<double>(nrm_all);
+        return;
+    }
+    if (MODE == 2) {
+        bool nonfinite = !isfinite(nrm_all);
+        // DGKS: one more pass only when the projection cancelled more than 1 - 1/sqrt(2).
+        const bool reorth = a.always_reorth || !(nrm_all >= T(0.70710678118654752) * static_cast<T>(ctl->wnorm));
+        ctl->reorth = reorth && !nonfinite ? 1 : 0;
+        if (ctl->reorth)
+            return;
+        for (int j = 0; j <= kcol; ++j) {
+            col[j] = a.h1[j];
+            nonfinite |= !isfinite(col[j]);
+        }
+        finish_column(ctl, a.H, a.hld, a.cs, a.sn, a.g, a.s, nrm_all, nonfinite);
+        return;
+    }
+    // MODE 3
+    bool nonfinite = !isfinite(nrm_all);
+    for (int j = 0; j <= kcol; ++j) {
+        col[j] = a.h1[j] + a.h2[j];
+        nonfinite |= !isfinite(col[j]);
+    }
+    ctl->reorth_count += 1;
+    finish_column(ctl, a.H, a.hld, a.cs, a.sn, a.g, a.s, nrm_all, nonfinite);
+}
+
+// y = s_k * (A W_k) with W_k gathered from the tile-major basis; G lanes per row.
+template <class T, int G>
+__global__ void __launch_bounds__(256) spmv_basis_kernel(int n, const int *__restrict__ rp,
+                                                         const int *__restrict__ ci,
+                                                         const T *__restrict__ av, Basis<T> V,
+                                                         T *__restrict__ y, const Ctl *ctl) {
+    constexpr int R = TileGeom<T>::R;
+    if (!ctl->active)
+        return;
+    const int k = ctl->k;
+    const T sk = V.scale[k];
+    const T *base = V.base + static_cast<long long>(k) * R;
+    const long long tstride = static_cast<long long>(V.cap1) * R;
+    const int lane = threadIdx.x & (G - 1);
+    const int groups = (gridDim.x * blockDim.x) / G;
+    const int warp_first = (blockIdx.x * blockDim.x + (threadIdx.x & ~31)) / G;
+    const int sub = (threadIdx.x & 31) / G;
+    for (int b0 = warp_first; b0 < n; b0 += groups) {
+        const int row = b0 + sub;
+        T acc = 0;
+        if (row < n)
+            for (int t = rp[row] + lane; t < rp[row + 1]; t += G) {
+                const int c = ci[t];
+                acc += av[t] * __ldg(base + (c / R) * tstride + (c % R));
+            }
+        for (int o = G / 2; o > 0; o >>= 1)
+            acc += __shfl_xor_sync(0xffffffffu, acc, o, G);
+        if (lane == 0 && row < n)
+            y[row] = acc * sk;
+    }
+}
+
+// x = sum_{j < count} (y_j s_j) W_j (candidate correction; x0 = 0).
+template <class T>
+__global__ void __launch_bounds__(256) form_candidate_tiles_kernel(int n, Basis<T> V, const T *y,
+                                                                   T *x, const Ctl *ctl) {
+    constexpr int R = TileGeom<T>::R;
+    if (!ctl->active || !ctl->vgate)
+        return;
+    const int count = ctl->formed;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const T *p = V.base + (static_cast<long long>(i / R) * V.cap1) * R + (i % R);
+        T acc = 0;
+#pragma unroll 8
+        for (int j = 0; j < count; ++j)
+            acc += (y[j] * V.scale[j]) * p[static_cast<long long>(j) * R];
+        x[i] = acc;
+    }
+}
+
+// W_0 = Pb / ||Pb|| into the tile-major basis, s_0 = 1; pad rows of every segment zeroed once
+// per solve so partial last tiles read zeros.
+template <class T>
+__global__ void __launch_bounds__(256) basis_start_kernel(int n, Basis<T> V, const T *pb, T *s,
+                                                          const Ctl *ctl) {
+    constexpr int R = TileGeom<T>::R;
+    if (!ctl->active)
+        return;
+    const T d = static_cast<T>(ctl->den);
+    const int padded = V.ntiles * R;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < padded; i += gridDim.x * blockDim.x) {
+        V.seg(i / R, 0)[i % R] = i < n ? pb[i] / d : T(0);
+        if (i == 0)
+            s[0] = T(1);
+    }
+}
+// Zero the pad rows (beyond n) of every segment of the last tile.
+template <class T> __global__ void basis_pad_kernel(int n, Basis<T> V) {
+    constexpr int R = TileGeom<T>::R;
+    const int t = V.ntiles - 1;
+    const int rows = n - t * R;
+    for (int j = blockIdx.x; j < V.cap1; j += gridDim.x)
+        for (int r = rows + threadIdx.x; r < R; r += blockDim.x)
+            V.seg(t, j)[r] = T(0);
+}
+
+} // namespace spai

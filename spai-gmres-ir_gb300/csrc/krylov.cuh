@@ -34,6 +34,9 @@ struct Ctl {
     int pending;      // an update x_new = x + d awaits its diagnostics
     int guard;        // Arnoldi steps run in this solve (bounds every device-side loop)
     int verifications; // candidate checks run in this solve
+    int reorth;        // this step needs the second Gram-Schmidt pass (DGKS criterion)
+    int reorth_count;  // second passes run in this solve
+    double wnorm;      // ||P A v_k|| before orthogonalisation
     double be, cbe, rinf, xinf, bscale, anorm_inf, binf;
     double inner_scale; // power of two applied to the correction right-hand side
     double tol_inner;

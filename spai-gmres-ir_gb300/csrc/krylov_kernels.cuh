@@ -20,6 +20,7 @@
 #include "exact_math.cuh"
 #pragma once
 #include "krylov.cuh"
+#include "cgs_tiles.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -202,170 +203,6 @@ __global__ void __launch_bounds__(kBlock) norm_kernel(int n, VecRef<T> ar, const
 }
 } // namespace kdetail
 
-// ------------------------------------------------------------------------------------------
-// Arnoldi passes.
-// ------------------------------------------------------------------------------------------
-// dots: part[b*ps + j] = sum over the block's rows of V_j[i] * w[i], j = 0..k. Last block
-// reduces into h[j]. Grid-stride over row tiles, one warp per basis vector within a tile.
-template <class T, int TILE>
-__global__ void __launch_bounds__(kBlock) arnoldi_dots_kernel(int n, long long ld, const T *V,
-                                                              const T *w, const Ctl *ctl, T *part,
-                                                              int ps, T *h, int *counter) {
-    if (!ctl->active)
-        return;
-    extern __shared__ __align__(16) unsigned char dyn[];
-    T *acc = reinterpret_cast<T *>(dyn); // [k+1]
-    __shared__ T wt[TILE];
-    const int k = ctl->k;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    for (int j = threadIdx.x; j <= k; j += blockDim.x)
-        acc[j] = 0;
-    for (long long r0 = static_cast<long long>(blockIdx.x) * TILE; r0 < n;
-         r0 += static_cast<long long>(gridDim.x) * TILE) {
-        const int rows = static_cast<int>(min(static_cast<long long>(TILE), n - r0));
-        __syncthreads();
-        for (int i = threadIdx.x; i < TILE; i += blockDim.x)
-            wt[i] = i < rows ? w[r0 + i] : T(0);
-        __syncthreads();
-        for (int j = warp; j <= k; j += nw) {
-            const T *vj = V + static_cast<long long>(j) * ld + r0;
-            T s = 0;
-#pragma unroll 4
-            for (int i = lane; i < rows; i += 32)
-                s += vj[i] * wt[i];
-            for (int o = 16; o > 0; o >>= 1)
-                s += __shfl_xor_sync(0xffffffffu, s, o);
-            if (lane == 0)
-                acc[j] += s;
-        }
-    }
-    __syncthreads();
-    for (int j = threadIdx.x; j <= k; j += blockDim.x)
-        part[static_cast<long long>(blockIdx.x) * ps + j] = acc[j];
-    if (!last_block(counter))
-        return;
-    for (int j = threadIdx.x; j <= k; j += blockDim.x) {
-        T s = 0;
-        for (int b = 0; b < static_cast<int>(gridDim.x); ++b)
-            s += part[static_cast<long long>(b) * ps + j];
-        h[j] = s;
-    }
-}
-
-// update: w[i] -= sum_j V_j[i] h[j]; optionally accumulate the norm partial of the new w and,
-// in the last block, finish the Arnoldi column: H(:,k) = h1 + h2, h(k+1,k) = ||w||, Givens.
-template <class T>
-__global__ void __launch_bounds__(kBlock) arnoldi_update_kernel(int n, long long ld, const T *V,
-                                                                T *w, Ctl *ctl, const T *h,
-                                                                NormPart *npart, int *counter,
-                                                                int finish, const T *h1, T *H,
-                                                                int hld, T *cs, T *sn, T *g) {
-    if (!ctl->active)
-        return;
-    __shared__ T sh[32];
-    __shared__ double shd[32];
-    __shared__ int be;
-    const int k = ctl->k;
-    const int stride = gridDim.x * blockDim.x;
-    T mx = 0;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        T acc = w[i];
-#pragma unroll 8
-        for (int j = 0; j <= k; ++j)
-            acc -= V[static_cast<long long>(j) * ld + i] * h[j];
-        w[i] = acc;
-        mx = fmax(mx, fabs(acc));
-    }
-    if (!finish)
-        return;
-    const T bmax = block_reduce_max(mx, sh);
-    if (threadIdx.x == 0)
-        be = exp_of(bmax);
-    __syncthreads();
-    double s = 0;
-    if (be != INT_MIN) {
-        const T scale = ldexp(T(1), -be);
-        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-            const T v = w[i] * scale;
-            s += static_cast<double>(v) * static_cast<double>(v);
-        }
-    }
-    const double bs = block_reduce_sum(s, shd);
-    if (threadIdx.x == 0)
-        npart[blockIdx.x] = NormPart{be, bs};
-    if (!last_block(counter))
-        return;
-    if (threadIdx.x != 0)
-        return;
-    // ---- Arnoldi column k and Givens update (src/gmres.cpp:174-214) ----
-    int E = INT_MIN;
-    bool nonfinite = !isfinite(static_cast<double>(bmax));
-    for (int b = 0; b < static_cast<int>(gridDim.x); ++b) {
-        E = max(E, npart[b].e);
-        nonfinite |= !isfinite(npart[b].s);
-    }
-    double S = 0;
-    if (E != INT_MIN)
-        for (int b = 0; b < static_cast<int>(gridDim.x); ++b)
-            if (npart[b].e != INT_MIN)
-                S += ldexp(npart[b].s, 2 * (npart[b].e - E));
-    const T hnext = E == INT_MIN ? T(0) : static_cast<T>(ldexp(sqrt(S), E));
-    T *col = H + static_cast<long long>(k) * hld;
-    for (int j = 0; j <= k; ++j) {
-        col[j] = h1[j] + h[j];
-        nonfinite |= !isfinite(col[j]);
-    }
-    col[k + 1] = hnext;
-    nonfinite |= !isfinite(hnext);
-    ctl->hnext = static_cast<double>(hnext);
-    ctl->breakdown = hnext == T(0);
-    for (int r = 0; r < k; ++r) {
-        const T up = col[r], lo = col[r + 1];
-        col[r] = cs[r] * up + sn[r] * lo;
-        col[r + 1] = -sn[r] * up + cs[r] * lo;
-    }
-    const T upper = col[k];
-    const T radius = cr_hypot<T>(upper, col[k + 1]);
-    ctl->iterations = k + 1;
-    if (nonfinite || !isfinite(radius)) {
-        ctl->status = 8; // numerical_failure
-        ctl->active = 0;
-        ctl->triggered = 0;
-        ctl->vgate = 0;
-        return;
-    }
-    if (radius == T(0)) {
-        // Zero Givens pivot: verify the previously defined candidate (gmres.cpp:218-234).
-        ctl->triggered = 2;
-        ctl->vgate = 1;
-        return;
-    }
-    cs[k] = upper / radius;
-    sn[k] = col[k + 1] / radius;
-    col[k] = radius;
-    col[k + 1] = 0;
-    const T old = g[k];
-    g[k] = cs[k] * old;
-    g[k + 1] = -sn[k] * old;
-    const T est = fabs(g[k + 1]) / static_cast<T>(ctl->den);
-    ctl->est = static_cast<double>(est);
-    const bool trig = ctl->breakdown || est <= static_cast<T>(ctl->tol_inner) || k + 1 == ctl->cap;
-    ctl->triggered = trig ? 1 : 0;
-    ctl->vgate = (trig || ctl->accept_every) ? 1 : 0;
-}
-
-// v_{k+1} = w / h(k+1,k) (skipped on breakdown).
-template <class T>
-__global__ void __launch_bounds__(kBlock) normalize_kernel(int n, long long ld, T *V, const T *w,
-                                                           const Ctl *ctl) {
-    if (!ctl->active || ctl->breakdown || ctl->triggered == 2 || ctl->status == 8)
-        return;
-    const T h = static_cast<T>(ctl->hnext);
-    T *v = V + static_cast<long long>(ctl->k + 1) * ld;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-        v[i] = w[i] / h;
-}
-
 // Back substitution y = R^{-1} g over `count` columns (src/gmres.cpp:47-55); count = k+1, or k
 // when the zero-pivot branch re-verifies the previous candidate. One block.
 template <class T>
@@ -388,22 +225,6 @@ __global__ void solve_y_kernel(Ctl *ctl, const T *H, int hld, const T *g, T *y) 
             ctl->status = 8;
             ctl->active = 0;
         }
-    }
-}
-
-// x = sum_j y_j V_j over the formed columns (x0 = 0 in every correction solve).
-template <class T>
-__global__ void __launch_bounds__(kBlock) form_candidate_kernel(int n, long long ld, const T *V,
-                                                                const T *y, T *x, const Ctl *ctl) {
-    if (!ctl->active || !ctl->vgate)
-        return;
-    const int count = ctl->formed;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        T acc = 0;
-#pragma unroll 8
-        for (int j = 0; j < count; ++j)
-            acc += V[static_cast<long long>(j) * ld + i] * y[j];
-        x[i] = acc;
     }
 }
 
@@ -522,16 +343,6 @@ __global__ void gmres_den_kernel(Ctl *ctl, const T *den, T *g, int accept_every)
     }
     g[0] = static_cast<T>(d);
 }
-template <class T>
-__global__ void __launch_bounds__(kBlock) scale_into_kernel(int n, const T *src, T *dst,
-                                                            const Ctl *ctl) {
-    if (!ctl->active)
-        return;
-    const T d = static_cast<T>(ctl->den);
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-        dst[i] = src[i] / d;
-}
-
 // ------------------------------------------------------------------------------------------
 // Iterative refinement in TO (binary64 for F64/MIXED, binary32 for F32).
 // ------------------------------------------------------------------------------------------
@@ -867,14 +678,17 @@ template <class T, class TO> struct IrEngine {
     const DeviceCsr<T> *a_inner = nullptr;
     const DeviceCsr<T> *p = nullptr;
     Ctl *ctl = nullptr;
-    T *V = nullptr, *w = nullptr, *t = nullptr, *rhs = nullptr, *pb = nullptr, *cand = nullptr,
+    T *V = nullptr, *sc = nullptr, *w = nullptr, *t = nullptr, *rhs = nullptr, *pb = nullptr, *cand = nullptr,
       *ax = nullptr, *pax = nullptr, *H = nullptr, *cs = nullptr, *sn = nullptr, *g = nullptr,
       *y = nullptr, *h1 = nullptr, *h2 = nullptr, *part = nullptr, *scal = nullptr;
     TO *r = nullptr, *xn = nullptr;
     NormPart *npart = nullptr;
     DiagPart *dpart = nullptr;
     int *counters = nullptr;
-    int nblk_vec = 0, nblk_dots = 0;
+    int nblk_vec = 0, nblk_dots = 0, ntiles = 0;
+    void *cgs_dots = nullptr, *cgs_norms = nullptr;
+    bool always_reorth = false;
+    int *pinned_host = nullptr; // host flag for profile-mode reads
     long long launches = 0;
     KernelProfile *prof = nullptr;
     int host_k = 0, solve_index = 0;
@@ -1008,9 +822,20 @@ template <class T, class TO> struct IrEngine {
         ld = (static_cast<long long>(n) + 31) & ~31LL;
         hld = cap + 2;
         nblk_vec = static_cast<int>(grid_for(n, kBlock, sms * 8));
-        nblk_dots = static_cast<int>(grid_for((n + 127) / 128, 1, sms * 4));
+        constexpr int R = TileGeom<T>::R;
+        ntiles = (n + R - 1) / R;
+        nblk_dots = std::min(ntiles, sms * 2);
         ctl = arena.alloc<Ctl>(1);
-        V = arena.alloc<T>(static_cast<size_t>(ld) * (cap + 1));
+        const size_t vcount = static_cast<size_t>(ntiles) * (cap + 1) * R;
+        V = arena.alloc<T>(vcount);
+        SPAI_CUDA(cudaMemset(V, 0, vcount * sizeof(T))); // pad rows of the last tile stay zero
+        sc = arena.alloc<T>(cap + 2);
+        cgs_dots = arena.alloc<T>(static_cast<size_t>(nblk_dots) * (cap + 2));
+        cgs_norms = arena.alloc<Ssq<T>>(nblk_dots);
+        const int smem = static_cast<int>(cgs_smem_for(cap));
+        SPAI_CUDA(cudaFuncSetAttribute(cgs_pass_kernel<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        SPAI_CUDA(cudaFuncSetAttribute(cgs_pass_kernel<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        SPAI_CUDA(cudaFuncSetAttribute(cgs_pass_kernel<T, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
         w = arena.alloc<T>(ld);
         t = arena.alloc<T>(ld);
         rhs = arena.alloc<T>(ld);
@@ -1040,8 +865,18 @@ template <class T, class TO> struct IrEngine {
     VecRef<T> fixed(T *p_) const {
         return VecRef<T>{p_, 0, nullptr, 0};
     }
-    VecRef<T> basis_at_k(int add) const {
-        return VecRef<T>{V, ld, &ctl->k, add};
+    Basis<T> basis() const {
+        return Basis<T>{V, cap + 1, ntiles, sc};
+    }
+    CgsArgs<T> cgs_args() const {
+        return CgsArgs<T>{n, basis(), w, h1, h2, H, cs, sn, g, sc, hld, ctl,
+                          CgsScratch{cgs_dots, cgs_norms, counters + kSlotDots}, always_reorth ? 1 : 0};
+    }
+    static size_t cgs_smem_for(int cap_) {
+        return sizeof(T) * (static_cast<size_t>(kCgsJB) * TileGeom<T>::R + TileGeom<T>::R + 2 * (cap_ + 2));
+    }
+    size_t cgs_smem() const {
+        return cgs_smem_for(cap);
     }
 
     void norm(cudaStream_t st, VecRef<T> a, const T *bsub, T *out, int slot, const int *gate) {
@@ -1069,39 +904,50 @@ template <class T, class TO> struct IrEngine {
     void arnoldi_passes(cudaStream_t st) {
         const double kk = host_k;
         timed(st, kClsSpmvA, spmv_bytes(*a_inner), [&] {
-            launch_spmv<T, T, T>(*a_inner, basis_at_k(0), fixed(t), &ctl->active, sms, st);
+            const int G = pick_group(*a_inner);
+            const unsigned blocks = grid_for(static_cast<long long>(n) * G, 256, sms * 16);
+            const Basis<T> vb = basis();
+#define SPAI_SPMV_BASIS(g)                                                                         \
+    case g:                                                                                        \
+        spmv_basis_kernel<T, g><<<blocks, 256, 0, st>>>(n, a_inner->rp, a_inner->ci, a_inner->val, \
+                                                        vb, t, ctl);                               \
+        break;
+            switch (G) {
+                SPAI_SPMV_BASIS(2)
+                SPAI_SPMV_BASIS(4)
+                SPAI_SPMV_BASIS(8)
+                SPAI_SPMV_BASIS(16)
+                SPAI_SPMV_BASIS(32)
+            }
+#undef SPAI_SPMV_BASIS
+            SPAI_LAUNCH("spmv_basis_kernel");
         });
         timed(st, kClsSpmvP, spmv_bytes(*p), [&] {
             launch_spmv<T, T, T>(*p, fixed(t), fixed(w), &ctl->active, sms, st);
         });
-        const size_t dyn = sizeof(T) * static_cast<size_t>(cap + 2);
+        const size_t smem = cgs_smem();
+        const CgsArgs<T> args = cgs_args();
         timed(st, kClsDots, vec_bytes(kk + 2), [&] {
-            arnoldi_dots_kernel<T, 128><<<nblk_dots, kBlock, dyn, st>>>(n, ld, V, w, ctl, part, cap + 2,
-                                                                         h1, counters + kSlotDots);
-            SPAI_LAUNCH("arnoldi_dots_kernel");
+            cgs_pass_kernel<T, 1><<<nblk_dots, kCgsThreads, smem, st>>>(args);
+            SPAI_LAUNCH("cgs_pass_kernel<1>");
         });
         timed(st, kClsUpdate, vec_bytes(kk + 3), [&] {
-            arnoldi_update_kernel<T><<<nblk_vec, kBlock, 0, st>>>(n, ld, V, w, ctl, h1, npart,
-                                                                   counters + kSlotUpdNorm, 0, nullptr,
-                                                                   H, hld, cs, sn, g);
-            SPAI_LAUNCH("arnoldi_update_kernel(1)");
+            cgs_pass_kernel<T, 2><<<nblk_dots, kCgsThreads, smem, st>>>(args);
+            SPAI_LAUNCH("cgs_pass_kernel<2>");
         });
-        timed(st, kClsDots, vec_bytes(kk + 2), [&] {
-            arnoldi_dots_kernel<T, 128><<<nblk_dots, kBlock, dyn, st>>>(n, ld, V, w, ctl, part, cap + 2,
-                                                                         h2, counters + kSlotDots);
-            SPAI_LAUNCH("arnoldi_dots_kernel(2)");
+        if (prof && prof->on && pinned_host) {
+            // Profile mode only: learn whether the DGKS pass runs, so that only real launches of
+            // the third pass are timed (it returns at once otherwise).
+            SPAI_CUDA(cudaMemcpyAsync(pinned_host, &ctl->reorth, sizeof(int), cudaMemcpyDeviceToHost, st));
+            SPAI_CUDA(cudaStreamSynchronize(st));
+            if (!*pinned_host)
+                return;
+        }
+        timed(st, kClsNormalize, vec_bytes(kk + 3), [&] {
+            cgs_pass_kernel<T, 3><<<nblk_dots, kCgsThreads, smem, st>>>(args);
+            SPAI_LAUNCH("cgs_pass_kernel<3>");
         });
-        timed(st, kClsUpdate, vec_bytes(kk + 3), [&] {
-            arnoldi_update_kernel<T><<<nblk_vec, kBlock, 0, st>>>(n, ld, V, w, ctl, h2, npart,
-                                                                   counters + kSlotUpdNorm, 1, h1, H,
-                                                                   hld, cs, sn, g);
-            SPAI_LAUNCH("arnoldi_update_kernel(2)");
-        });
-        timed(st, kClsNormalize, vec_bytes(2), [&] {
-            normalize_kernel<T><<<nblk_vec, kBlock, 0, st>>>(n, ld, V, w, ctl);
-            SPAI_LAUNCH("normalize_kernel");
-        });
-        launches += 7;
+        launches += 5;
     }
 
     void verify(cudaStream_t st) {
@@ -1114,8 +960,8 @@ template <class T, class TO> struct IrEngine {
     void verify_checks(cudaStream_t st) {
         solve_y_kernel<T><<<1, 32, 0, st>>>(ctl, H, hld, g, y);
         SPAI_LAUNCH("solve_y_kernel");
-        form_candidate_kernel<T><<<nblk_vec, kBlock, 0, st>>>(n, ld, V, y, cand, ctl);
-        SPAI_LAUNCH("form_candidate_kernel");
+        form_candidate_tiles_kernel<T><<<nblk_vec, kBlock, 0, st>>>(n, basis(), y, cand, ctl);
+        SPAI_LAUNCH("form_candidate_tiles_kernel");
         const int *g2 = &ctl->vgate;
         launch_spmv<T, T, T>(*a_inner, fixed(cand), fixed(ax), g2, sms, st);
         norm(st, fixed(rhs), ax, scal + 0, kSlotNormA, g2);
@@ -1133,8 +979,8 @@ template <class T, class TO> struct IrEngine {
         norm(st, fixed(pb), nullptr, scal + 3, kSlotNormB, &ctl->active);
         gmres_den_kernel<T><<<1, 32, 0, st>>>(ctl, scal + 3, g, accept_every ? 1 : 0);
         SPAI_LAUNCH("gmres_den_kernel");
-        scale_into_kernel<T><<<nblk_vec, kBlock, 0, st>>>(n, pb, V, ctl);
-        SPAI_LAUNCH("scale_into_kernel");
+        basis_start_kernel<T><<<nblk_vec, kBlock, 0, st>>>(n, basis(), pb, sc, ctl);
+        SPAI_LAUNCH("basis_start_kernel");
         launches += 4;
     }
 
@@ -1148,6 +994,7 @@ template <class T, class TO> struct IrEngine {
     // solve ends are no-ops gated on ctl->active).
     void gmres_loop(cudaStream_t st, bool accept_every, int *pinned) {
         (void)accept_every;
+        pinned_host = pinned + 1;
         const int batch = 8;
         host_k = 0;
         for (int it = 0; it < cap; it += batch) {

@@ -18,6 +18,7 @@
 #include "exact_math.cuh"
 #include "spai_internal.hpp"
 
+#include <cooperative_groups.h>
 #include <cub/device/device_scan.cuh>
 
 #include <algorithm>
@@ -116,8 +117,11 @@ __global__ void column_fill_kernel(int n, const int *__restrict__ rp, const int 
 }
 
 // ------------------------------------------------------------------------------------------
-// Warp-cooperative building blocks (all lanes of the warp call them together).
+// Group-cooperative building blocks: a group of G lanes (a thread_block_tile<G>) owns a column;
+// 32/G columns run in each warp. Every function is called by all lanes of the group together.
 // ------------------------------------------------------------------------------------------
+namespace cg = cooperative_groups;
+
 struct Bump {
     char *base;
     size_t cap, top;
@@ -144,12 +148,38 @@ __device__ __forceinline__ int pow2_at_least(int x) {
     return p;
 }
 
+template <class Grp> __device__ __forceinline__ int grp_sum(const Grp &g, int v) {
+    for (int o = Grp::size() / 2; o > 0; o >>= 1)
+        v += g.shfl_xor(v, o);
+    return v;
+}
+template <class Grp> __device__ __forceinline__ int grp_min(const Grp &g, int v) {
+    for (int o = Grp::size() / 2; o > 0; o >>= 1)
+        v = min(v, g.shfl_xor(v, o));
+    return v;
+}
+template <class Grp, class T> __device__ __forceinline__ T grp_fmax(const Grp &g, T v) {
+    for (int o = Grp::size() / 2; o > 0; o >>= 1)
+        v = fmax(v, g.shfl_xor(v, o));
+    return v;
+}
+template <class Grp> __device__ __forceinline__ int grp_inclusive_scan(const Grp &g, int v) {
+    const int r = g.thread_rank();
+    for (int o = 1; o < static_cast<int>(Grp::size()); o <<= 1) {
+        const int t = g.shfl_up(v, o);
+        if (r >= o)
+            v += t;
+    }
+    return v;
+}
+
 // Ascending bitonic sort of a[0..N), N a power of two.
-__device__ void warp_bitonic_sort(int *a, int N) {
-    const int lane = lane_id();
+template <class Grp> __device__ void grp_bitonic_sort(const Grp &g, int *a, int N) {
+    const int r = g.thread_rank();
+    constexpr int GS = Grp::size();
     for (int size = 2; size <= N; size <<= 1) {
         for (int stride = size >> 1; stride > 0; stride >>= 1) {
-            for (int t = lane; t < (N >> 1); t += 32) {
+            for (int t = r; t < (N >> 1); t += GS) {
                 const int i = 2 * t - (t & (stride - 1));
                 const int j = i + stride;
                 const bool asc = (i & size) == 0;
@@ -159,23 +189,24 @@ __device__ void warp_bitonic_sort(int *a, int N) {
                     a[j] = x;
                 }
             }
-            __syncwarp();
+            g.sync();
         }
     }
 }
 
 // In-place unique of sorted a[0..L) also dropping members of sorted ex[0..ne). Returns count.
-__device__ int warp_unique_except(int *a, int L, const int *ex, int ne) {
-    const int lane = lane_id();
+template <class Grp> __device__ int grp_unique_except(const Grp &g, int *a, int L, const int *ex, int ne) {
+    const int r = g.thread_rank();
+    constexpr int GS = Grp::size();
     int out = 0;
     int prev_carry = INT_MIN;
-    for (int base = 0; base < L; base += 32) {
-        const int t = base + lane;
+    for (int base = 0; base < L; base += GS) {
+        const int t = base + r;
         int val = 0;
         bool keep = false;
         if (t < L) {
             val = a[t];
-            const int prev = t == 0 ? INT_MIN : (lane == 0 ? prev_carry : a[t - 1]);
+            const int prev = t == 0 ? INT_MIN : (r == 0 ? prev_carry : a[t - 1]);
             keep = (t == 0 || val != prev);
             if (keep && ne > 0) {
                 int lo = 0, hi = ne;
@@ -189,14 +220,14 @@ __device__ int warp_unique_except(int *a, int L, const int *ex, int ne) {
                 keep = !(lo < ne && ex[lo] == val);
             }
         }
-        const int last_in_chunk = min(L, base + 32) - 1;
+        const int last_in_chunk = min(L, base + GS) - 1;
         prev_carry = a[last_in_chunk];
-        __syncwarp();
-        const unsigned bal = __ballot_sync(0xffffffffu, keep);
+        g.sync();
+        const unsigned bal = g.ballot(keep);
         if (keep)
-            a[out + __popc(bal & ((1u << lane) - 1))] = val;
+            a[out + __popc(bal & ((1u << r) - 1))] = val;
         out += __popc(bal);
-        __syncwarp();
+        g.sync();
     }
     return out;
 }
@@ -230,86 +261,121 @@ template <class T> struct ColumnArgs {
     T *packed_val;
     unsigned long long *packed_top;
     unsigned long long packed_cap;
-    int *queue;        // [0] next column (main pass), [1] overflow count, [2] next overflow
-    int *overflow_list;
+    int *queue;        // [0] next column, [1] list-1 size, [2] next in list 1, [3] list-2 size, [4] next in list 2
+    int *overflow_list, *overflow_list2;
     int *error;        // bit0 packed output full, bit1 column exceeded the largest workspace
 };
 
 // Gather the dense reduced matrix R = B(I, J) (row-major m x q): R[i*q+jj] = A(J[jj], I[i]) d_J.
-template <class T>
-__device__ void gather_reduced(const ColumnArgs<T> &A, const int *J, int q, const int *I, int m,
-                               T *R) {
-    const int lane = lane_id();
-    for (long long t = lane; t < static_cast<long long>(m) * q; t += 32)
+template <class Grp, class T>
+__device__ void gather_reduced(const Grp &g, const ColumnArgs<T> &A, const int *J, int q,
+                               const int *I, int m, T *R) {
+    const int r = g.thread_rank();
+    constexpr int GS = Grp::size();
+    for (long long t = r; t < static_cast<long long>(m) * q; t += GS)
         R[t] = T(0);
-    __syncwarp();
+    g.sync();
     for (int jj = 0; jj < q; ++jj) {
         const int j = J[jj];
         const int b = A.rp[j], e = A.rp[j + 1];
         const T dj = A.d[j];
-        for (int t = b + lane; t < e; t += 32) {
+        for (int t = b + r; t < e; t += GS) {
             const int pos = lower_bound_int(I, m, A.ci[t]);
             R[static_cast<long long>(pos) * q + jj] = A.av[t] * dj;
         }
     }
-    __syncwarp();
+    g.sync();
+}
+
+// Fast-mode 2-norm of x[0..m) (stride st): power-of-two scaling by the group max, then a group
+// sum of squares. Overflow-safe; the summation order is a tree, not the reference's chain.
+template <class Grp, class T>
+__device__ T grp_norm(const Grp &g, const T *x, int m, long long stride) {
+    constexpr int GS = Grp::size();
+    T mx = 0;
+    for (int i = g.thread_rank(); i < m; i += GS)
+        mx = fmax(mx, fabs(x[i * stride]));
+    mx = grp_fmax(g, mx);
+    if (!(mx > T(0)) || !isfinite(mx))
+        return mx > T(0) ? mx : T(0);
+    const int e = ilogb(mx);
+    T acc = 0;
+    for (int i = g.thread_rank(); i < m; i += GS) {
+        const T v = ldexp(x[i * stride], -e);
+        acc += v * v;
+    }
+    for (int o = GS / 2; o > 0; o >>= 1)
+        acc += g.shfl_xor(acc, o);
+    return ldexp(sqrt(acc), e);
 }
 
 // Householder least squares with normalised reflectors, src/spai.cpp:30-98. R is destroyed,
 // rhs is transformed, coef receives the solution. Returns a SpaiStatus code.
-template <class T>
-__device__ int warp_least_squares(T *R, T *rhs, int m, int q, T *coef, T *v, T &pivot_ratio) {
-    const int lane = lane_id();
+template <bool FAST, class Grp, class T>
+__device__ int grp_least_squares(const Grp &g, T *R, T *rhs, int m, int q, T *coef, T *v,
+                                 T &pivot_ratio) {
+    const int lane = g.thread_rank();
+    constexpr int GS = Grp::size();
     if (m < q)
         return kRankDeficient;
     // Infinity norm: sequential row sums, max over rows (max is order independent).
     T inf_norm = 0;
-    for (int i = lane; i < m; i += 32) {
+    for (int i = lane; i < m; i += GS) {
         T sum = 0;
         for (int j = 0; j < q; ++j)
             sum += fabs(R[static_cast<long long>(i) * q + j]);
         inf_norm = fmax(inf_norm, sum);
     }
-    for (int o = 16; o > 0; o >>= 1)
-        inf_norm = fmax(inf_norm, __shfl_xor_sync(0xffffffffu, inf_norm, o));
+    inf_norm = grp_fmax(g, inf_norm);
     T min_pivot = T(INFINITY);
     for (int j = 0; j < q; ++j) {
         T length = 0;
-        if (lane == 0)
-            for (int i = j; i < m; ++i)
-                length = cr_hypot(length, R[static_cast<long long>(i) * q + j]);
-        length = shfl(length, 0);
+        if (FAST) {
+            length = grp_norm(g, R + static_cast<long long>(j) * q + j, m - j, q);
+        } else {
+            if (lane == 0)
+                for (int i = j; i < m; ++i)
+                    length = cr_hypot(length, R[static_cast<long long>(i) * q + j]);
+            length = g.shfl(length, 0);
+        }
         if (!isfinite(length))
             return kNumericalFailure;
         if (length == T(0))
             return kRankDeficient;
         const T x0 = R[static_cast<long long>(j) * q + j];
         const T diagonal = -copysign(length, x0);
-        for (int i = j + lane; i < m; i += 32)
+        for (int i = j + lane; i < m; i += GS)
             v[i - j] = R[static_cast<long long>(i) * q + j] / length;
-        __syncwarp();
+        g.sync();
         T vnorm = 0;
-        if (lane == 0) {
-            v[0] += copysign(T(1), v[0]);
-            for (int i = 0; i < m - j; ++i)
-                vnorm = cr_hypot(vnorm, v[i]);
+        if (FAST) {
+            // |v|^2 = sum (x_i/L)^2 + 2|x_0|/L + 1 = 2 (1 + |x_0|/L) for the shifted reflector.
+            if (lane == 0)
+                v[0] += copysign(T(1), v[0]);
+            vnorm = sqrt(T(2) * (T(1) + fabs(x0) / length));
+        } else {
+            if (lane == 0) {
+                v[0] += copysign(T(1), v[0]);
+                for (int i = 0; i < m - j; ++i)
+                    vnorm = cr_hypot(vnorm, v[i]);
+            }
+            vnorm = g.shfl(vnorm, 0);
         }
-        vnorm = shfl(vnorm, 0);
-        __syncwarp();
-        for (int i = lane; i < m - j; i += 32)
+        g.sync();
+        for (int i = lane; i < m - j; i += GS)
             v[i] /= vnorm;
-        __syncwarp();
+        g.sync();
         // Columns j..q-1 of R and the right-hand side (as column q) in parallel, one per lane.
         int bad = 0;
-        for (int col = j + lane; col <= q; col += 32) {
+        for (int col = j + lane; col <= q; col += GS) {
             T dot = 0;
             if (col < q) {
                 for (int i = j; i < m; ++i)
                     dot += v[i - j] * R[static_cast<long long>(i) * q + col];
                 for (int i = j; i < m; ++i) {
-                    T &r = R[static_cast<long long>(i) * q + col];
-                    r -= 2 * v[i - j] * dot;
-                    bad |= !isfinite(r);
+                    T &rr = R[static_cast<long long>(i) * q + col];
+                    rr -= 2 * v[i - j] * dot;
+                    bad |= !isfinite(rr);
                 }
             } else {
                 for (int i = j; i < m; ++i)
@@ -320,12 +386,12 @@ __device__ int warp_least_squares(T *R, T *rhs, int m, int q, T *coef, T *v, T &
                 }
             }
         }
-        if (__any_sync(0xffffffffu, bad))
+        if (g.any(bad))
             return kNumericalFailure;
-        __syncwarp();
+        g.sync();
         if (lane == 0)
             R[static_cast<long long>(j) * q + j] = diagonal;
-        __syncwarp();
+        g.sync();
         min_pivot = fmin(min_pivot, fabs(diagonal));
     }
     pivot_ratio = inf_norm == T(0) ? T(0) : min_pivot / inf_norm;
@@ -351,8 +417,8 @@ __device__ int warp_least_squares(T *R, T *rhs, int m, int q, T *coef, T *v, T &
             }
         }
     }
-    st = shfl(st, 0);
-    __syncwarp();
+    st = g.shfl(st, 0);
+    g.sync();
     return st;
 }
 
@@ -393,9 +459,10 @@ __global__ void score_kat_kernel(T rsq, T dot, T den, double *out) {
 
 // One adaptive column (src/spai.cpp:100-244). Returns a final SpaiStatus or kOverflow when the
 // workspace (ws, cap bytes; J capacity qcap) is too small for this column.
-template <class T>
-__device__ int fit_column(const ColumnArgs<T> &A, int k, char *ws, size_t cap, int qcap) {
-    const int lane = lane_id();
+template <bool FAST, class Grp, class T>
+__device__ int fit_column(const Grp &g, const ColumnArgs<T> &A, int k, char *ws, size_t cap, int qcap) {
+    const int lane = g.thread_rank();
+    constexpr int GS = Grp::size();
     int *J = reinterpret_cast<int *>(ws);
     int *lastJ = J + qcap;
     T *lastC = reinterpret_cast<T *>(ws + ((static_cast<size_t>(2 * qcap) * 4 + 15) & ~size_t(15)));
@@ -407,7 +474,7 @@ __device__ int fit_column(const ColumnArgs<T> &A, int k, char *ws, size_t cap, i
     int q = 1;
     if (lane == 0)
         J[0] = k;
-    __syncwarp();
+    g.sync();
     int fits = 0, growths = 0, clamps = 0, lastq = 0;
     T last_res = T(NAN);
     int status = kNotAttempted;
@@ -416,9 +483,9 @@ __device__ int fit_column(const ColumnArgs<T> &A, int k, char *ws, size_t cap, i
         bump.reset(0);
         // ---- shadow I: union of the row patterns of A over J ----
         int L1 = 0;
-        for (int t = lane; t < q; t += 32)
+        for (int t = lane; t < q; t += GS)
             L1 += A.rp[J[t] + 1] - A.rp[J[t]];
-        L1 = warp_sum_int(L1);
+        L1 = grp_sum(g, L1);
         const int P1 = pow2_at_least(max(L1, 1));
         int *I = bump.take<int>(P1);
         if (!I)
@@ -428,16 +495,16 @@ __device__ int fit_column(const ColumnArgs<T> &A, int k, char *ws, size_t cap, i
             for (int jj = 0; jj < q; ++jj) {
                 const int j = J[jj];
                 const int b = A.rp[j], len = A.rp[j + 1] - b;
-                for (int t = lane; t < len; t += 32)
+                for (int t = lane; t < len; t += GS)
                     I[off + t] = A.ci[b + t];
                 off += len;
             }
-            for (int t = L1 + lane; t < P1; t += 32)
+            for (int t = L1 + lane; t < P1; t += GS)
                 I[t] = INT_MAX;
-            __syncwarp();
+            g.sync();
         }
-        warp_bitonic_sort(I, P1);
-        const int m = warp_unique_except(I, L1, nullptr, 0);
+        grp_bitonic_sort(g, I, P1);
+        const int m = grp_unique_except(g, I, L1, static_cast<const int *>(nullptr), 0);
         bump.reset(static_cast<size_t>(m) * 4);
         if (m < q) {
             status = kRankDeficient;
@@ -451,20 +518,20 @@ __device__ int fit_column(const ColumnArgs<T> &A, int k, char *ws, size_t cap, i
         T *coef = bump.take<T>(q);
         if (!s || !R || !rhs || !v || !coef)
             return kOverflow;
-        gather_reduced(A, J, q, I, m, R);
-        for (int i = lane; i < m; i += 32)
+        gather_reduced(g, A, J, q, I, m, R);
+        for (int i = lane; i < m; i += GS)
             rhs[i] = I[i] == k ? T(1) : T(0);
-        __syncwarp();
+        g.sync();
         T pivot_ratio = 0;
-        const int ls = warp_least_squares(R, rhs, m, q, coef, v, pivot_ratio);
+        const int ls = grp_least_squares<FAST>(g, R, rhs, m, q, coef, v, pivot_ratio);
         if (ls != kSuccess) {
             status = ls;
             break;
         }
         // Fitted residual with the original reduced matrix.
-        gather_reduced(A, J, q, I, m, R);
+        gather_reduced(g, A, J, q, I, m, R);
         int bad = 0;
-        for (int i = lane; i < m; i += 32) {
+        for (int i = lane; i < m; i += GS) {
             T acc = 0;
             for (int jj = 0; jj < q; ++jj)
                 acc += R[static_cast<long long>(i) * q + jj] * coef[jj];
@@ -472,16 +539,20 @@ __device__ int fit_column(const ColumnArgs<T> &A, int k, char *ws, size_t cap, i
             s[i] = acc;
             bad |= !isfinite(acc);
         }
-        if (__any_sync(0xffffffffu, bad)) {
+        if (g.any(bad)) {
             status = kNumericalFailure;
             break;
         }
-        __syncwarp();
+        g.sync();
         T res = 0;
-        if (lane == 0)
-            for (int i = 0; i < m; ++i)
-                res = cr_hypot(res, s[i]);
-        res = shfl(res, 0);
+        if (FAST) {
+            res = grp_norm(g, s, m, 1);
+        } else {
+            if (lane == 0)
+                for (int i = 0; i < m; ++i)
+                    res = cr_hypot(res, s[i]);
+            res = g.shfl(res, 0);
+        }
         if (!isfinite(res)) {
             status = kNumericalFailure;
             break;
@@ -491,11 +562,11 @@ __device__ int fit_column(const ColumnArgs<T> &A, int k, char *ws, size_t cap, i
         ++fits;
         lastq = q;
         last_res = res;
-        for (int t = lane; t < q; t += 32) {
+        for (int t = lane; t < q; t += GS) {
             lastJ[t] = J[t];
             lastC[t] = coef[t];
         }
-        __syncwarp();
+        g.sync();
         if (res <= eps) {
             status = kSuccess;
             break;
@@ -507,37 +578,86 @@ __device__ int fit_column(const ColumnArgs<T> &A, int k, char *ws, size_t cap, i
         // ---- candidates: column patterns over I and k, minus J ----
         bump.reset(keep_mark);
         int L2 = 0;
-        for (int t = lane; t < m; t += 32)
+        for (int t = lane; t < m; t += GS)
             L2 += A.tp[I[t] + 1] - A.tp[I[t]];
-        L2 = warp_sum_int(L2) + (A.tp[k + 1] - A.tp[k]);
+        L2 = grp_sum(g, L2) + (A.tp[k + 1] - A.tp[k]);
+        int c = 0;
+        int *C = nullptr;
+        if (FAST) {
+            // Unique candidates through an open-addressing set (load factor <= 2/3); the order of
+            // the compacted list is irrelevant in this mode (parallel mean, index tie-break).
+            const int P2 = pow2_at_least(max(3 * L2 / 2 + 1, 2));
+            C = bump.take<int>(P2);
+            if (!C)
+                return kOverflow;
+            for (int t = lane; t < P2; t += GS)
+                C[t] = -1;
+            g.sync();
+            auto insert = [&](int x) {
+                unsigned h = (static_cast<unsigned>(x) * 2654435761u) & static_cast<unsigned>(P2 - 1);
+                for (int probe = 0; probe < P2; ++probe) {
+                    const int prev = atomicCAS(&C[h], -1, x);
+                    if (prev == -1 || prev == x)
+                        return;
+                    h = (h + 1) & static_cast<unsigned>(P2 - 1);
+                }
+            };
+            for (int t = 0; t < m; ++t) {
+                const int b = A.tp[I[t]], e = A.tp[I[t] + 1];
+                for (int x = b + lane; x < e; x += GS)
+                    insert(A.ti[x]);
+            }
+            for (int x = A.tp[k] + lane; x < A.tp[k + 1]; x += GS)
+                insert(A.ti[x]);
+            g.sync();
+            // Compact in place, dropping empty slots and members of J.
+            int out = 0;
+            for (int base = 0; base < P2; base += GS) {
+                const int t = base + lane;
+                int val = t < P2 ? C[t] : -1;
+                bool keep = val >= 0;
+                if (keep) {
+                    const int pos = lower_bound_int(J, q, val);
+                    keep = !(pos < q && J[pos] == val);
+                }
+                g.sync();
+                const unsigned bal = g.ballot(keep);
+                if (keep)
+                    C[out + __popc(bal & ((1u << lane) - 1))] = val;
+                out += __popc(bal);
+                g.sync();
+            }
+            c = out;
+        } else {
         const int P2 = pow2_at_least(max(L2, 1));
-        int *C = bump.take<int>(P2);
+        C = bump.take<int>(P2);
         if (!C)
             return kOverflow;
         {
             int base_off = 0;
-            for (int base = 0; base < m; base += 32) {
+            for (int base = 0; base < m; base += GS) {
                 const int t = base + lane;
                 int len = 0, b = 0;
                 if (t < m) {
                     b = A.tp[I[t]];
                     len = A.tp[I[t] + 1] - b;
                 }
-                const int incl = warp_inclusive_scan(len);
+                const int incl = grp_inclusive_scan(g, len);
                 const int start = base_off + incl - len;
                 for (int x = 0; x < len; ++x)
                     C[start + x] = A.ti[b + x];
-                base_off += shfl(incl, 31);
+                base_off += g.shfl(incl, GS - 1);
             }
             const int b = A.tp[k], len = A.tp[k + 1] - b;
-            for (int x = lane; x < len; x += 32)
+            for (int x = lane; x < len; x += GS)
                 C[base_off + x] = A.ti[b + x];
-            for (int t = L2 + lane; t < P2; t += 32)
+            for (int t = L2 + lane; t < P2; t += GS)
                 C[t] = INT_MAX;
-            __syncwarp();
+            g.sync();
         }
-        warp_bitonic_sort(C, P2);
-        const int c = warp_unique_except(C, L2, J, q);
+        grp_bitonic_sort(g, C, P2);
+        c = grp_unique_except(g, C, L2, J, q);
+        }
         if (c == 0) {
             status = kEmptyCandidates;
             break;
@@ -551,7 +671,7 @@ __device__ int fit_column(const ColumnArgs<T> &A, int k, char *ws, size_t cap, i
         // ---- scores: one lane per candidate, ascending shadow order ----
         const T rsq = res * res;
         int first_fail = INT_MAX, my_status = kSuccess, my_clamps = 0;
-        for (int t = lane; t < c; t += 32) {
+        for (int t = lane; t < c; t += GS) {
             const int j = C[t];
             const int b = A.rp[j], e = A.rp[j + 1];
             const T dj = A.d[j];
@@ -569,28 +689,36 @@ __device__ int fit_column(const ColumnArgs<T> &A, int k, char *ws, size_t cap, i
             int clamped;
             const int st = score_value<T>(rsq, dot, den, score, clamped);
             sc[t] = score;
-            if (st != kSuccess && t < first_fail) {
-                first_fail = t;
+            if (st != kSuccess && (FAST ? j : t) < first_fail) {
+                first_fail = FAST ? j : t;
                 my_status = st;
             }
             if (st == kSuccess && clamped)
                 my_clamps += 1;
         }
-        const int ff = warp_min_int(first_fail);
+        const int ff = grp_min(g, first_fail);
         if (ff != INT_MAX) {
-            const unsigned owner = __ballot_sync(0xffffffffu, first_fail == ff);
-            status = shfl(my_status, __ffs(owner) - 1);
+            const unsigned owner = g.ballot(first_fail == ff);
+            status = g.shfl(my_status, __ffs(owner) - 1);
             break;
         }
-        clamps += warp_sum_int(my_clamps);
-        __syncwarp();
+        clamps += grp_sum(g, my_clamps);
+        g.sync();
         T mean = 0;
-        if (lane == 0) {
-            for (int t = 0; t < c; ++t)
+        if (FAST) {
+            for (int t = lane; t < c; t += GS)
                 mean += sc[t];
+            for (int o = GS / 2; o > 0; o >>= 1)
+                mean += g.shfl_xor(mean, o);
             mean = mean / static_cast<T>(c);
+        } else {
+            if (lane == 0) {
+                for (int t = 0; t < c; ++t)
+                    mean += sc[t];
+                mean = mean / static_cast<T>(c);
+            }
+            mean = g.shfl(mean, 0);
         }
-        mean = shfl(mean, 0);
         if (!isfinite(mean)) {
             status = kNumericalFailure;
             break;
@@ -600,19 +728,25 @@ __device__ int fit_column(const ColumnArgs<T> &A, int k, char *ws, size_t cap, i
         for (; nsel < nsel_cap; ++nsel) {
             T best = T(INFINITY);
             int best_t = INT_MAX;
-            for (int t = lane; t < c; t += 32) {
+            // Ties go to the smaller candidate index (C is sorted in exact mode, so this is the
+            // reference's stable (score, index) order; in fast mode C is unordered).
+            int best_c = INT_MAX;
+            for (int t = lane; t < c; t += GS) {
                 const T x = sc[t];
-                if (x <= mean && (x < best || (x == best && t < best_t))) {
+                if (x <= mean && (x < best || (x == best && C[t] < best_c))) {
                     best = x;
                     best_t = t;
+                    best_c = C[t];
                 }
             }
-            for (int o = 16; o > 0; o >>= 1) {
-                const T ob = __shfl_xor_sync(0xffffffffu, best, o);
-                const int ot = __shfl_xor_sync(0xffffffffu, best_t, o);
-                if (ob < best || (ob == best && ot < best_t)) {
+            for (int o = GS / 2; o > 0; o >>= 1) {
+                const T ob = g.shfl_xor(best, o);
+                const int ot = g.shfl_xor(best_t, o);
+                const int oc = g.shfl_xor(best_c, o);
+                if (ob < best || (ob == best && oc < best_c)) {
                     best = ob;
                     best_t = ot;
+                    best_c = oc;
                 }
             }
             if (best_t == INT_MAX)
@@ -621,7 +755,7 @@ __device__ int fit_column(const ColumnArgs<T> &A, int k, char *ws, size_t cap, i
                 sel[nsel] = C[best_t];
                 sc[best_t] = T(INFINITY); // consumed
             }
-            __syncwarp();
+            g.sync();
         }
         if (nsel == 0) {
             status = kNoGrowth;
@@ -649,7 +783,7 @@ __device__ int fit_column(const ColumnArgs<T> &A, int k, char *ws, size_t cap, i
             }
         }
         q += nsel;
-        __syncwarp();
+        g.sync();
     }
     // ---- publish the last completed fit (column.pattern/coefficients) ----
     long long off = 0;
@@ -667,50 +801,61 @@ __device__ int fit_column(const ColumnArgs<T> &A, int k, char *ws, size_t cap, i
         A.residual[k] = last_res;
         A.out_off[k] = off;
     }
-    off = shfl(off, 0);
+    off = g.shfl(off, 0);
     if (off >= 0)
-        for (int t = lane; t < lastq; t += 32) {
+        for (int t = lane; t < lastq; t += GS) {
             A.packed_idx[off + t] = lastJ[t];
             A.packed_val[off + t] = lastC[t];
         }
     return status;
 }
 
-// Persistent column kernel. mode 0: all columns via the atomic queue, shared-memory workspace
-// of ws_bytes per warp; columns that do not fit go to the overflow list. mode 1: the overflow
-// list, global workspace gws of ws_bytes per warp.
-template <class T>
+// Persistent column kernel with G lanes per column (32/G columns per warp). mode 0: all columns
+// via the atomic queue, shared-memory workspace of ws_bytes per group; columns that do not fit go
+// to the overflow list. mode 1: the overflow list, global workspace gws of ws_bytes per group.
+template <class T, int G, bool FAST>
 __global__ void spai_columns_kernel(ColumnArgs<T> A, int mode, size_t ws_bytes, int qcap,
                                     char *gws) {
+    // mode 0: all columns from queue[0], shared workspace ws_bytes per group; misfits -> list 1.
+    // mode 2: list 1 from queue[2], one group per block using the block's shared memory; misfits
+    //         -> list 2 (queue[3]).
+    // mode 3: list 2 from queue[4], global workspace ws_bytes per group; misfits -> error.
     extern __shared__ __align__(16) char smem[];
-    const int warp = threadIdx.x >> 5;
-    const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    char *ws = mode == 0 ? smem + static_cast<size_t>(warp) * ws_bytes
-                         : gws + static_cast<size_t>(gwarp) * ws_bytes;
-    const int lane = lane_id();
+    const auto g = cg::tiled_partition<G>(cg::this_thread_block());
+    const int grp = threadIdx.x / G;
+    const int ggrp = (blockIdx.x * blockDim.x + threadIdx.x) / G;
+    char *ws = mode == 3 ? gws + static_cast<size_t>(ggrp) * ws_bytes
+                         : smem + static_cast<size_t>(grp) * ws_bytes;
+    const int lane = g.thread_rank();
     for (;;) {
         int slot = 0;
         if (lane == 0)
-            slot = atomicAdd(mode == 0 ? &A.queue[0] : &A.queue[2], 1);
-        slot = shfl(slot, 0);
+            slot = atomicAdd(mode == 0 ? &A.queue[0] : (mode == 2 ? &A.queue[2] : &A.queue[4]), 1);
+        slot = g.shfl(slot, 0);
         int k;
         if (mode == 0) {
             if (slot >= A.n)
                 break;
             k = slot;
-        } else {
+        } else if (mode == 2) {
             if (slot >= A.queue[1])
                 break;
             k = A.overflow_list[slot];
+        } else {
+            if (slot >= A.queue[3])
+                break;
+            k = A.overflow_list2[slot];
         }
-        const int r = fit_column(A, k, ws, ws_bytes, qcap);
+        const int r = fit_column<FAST>(g, A, k, ws, ws_bytes, qcap);
         if (r == kOverflow && lane == 0) {
             if (mode == 0)
                 A.overflow_list[atomicAdd(&A.queue[1], 1)] = k;
+            else if (mode == 2)
+                A.overflow_list2[atomicAdd(&A.queue[3], 1)] = k;
             else
                 atomicOr(A.error, 2);
         }
-        __syncwarp();
+        g.sync();
     }
 }
 
@@ -774,6 +919,58 @@ __global__ void stats_kernel(int n, const int *__restrict__ fits, const int *__r
 // ------------------------------------------------------------------------------------------
 // Host driver.
 // ------------------------------------------------------------------------------------------
+// Launch the column kernel for a group width G: `work` groups of G lanes in blocks of `threads`.
+// mode 0 sizes the grid to the SMs' resident capacity (persistent); mode 1 launches one block
+// per `per_block` groups.
+template <class T, int G, bool FAST>
+void launch_columns_g(ColumnArgs<T> args, int mode, size_t ws, int qcap, char *gws, size_t smem,
+                      int threads, long long work, int groups_per_block, int sms, cudaStream_t st) {
+    if (mode != 3) {
+        SPAI_CUDA(cudaFuncSetAttribute(spai_columns_kernel<T, G, FAST>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       static_cast<int>(smem)));
+        int per_sm = 0;
+        SPAI_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, spai_columns_kernel<T, G, FAST>,
+                                                                threads, smem));
+        if (per_sm < 1)
+            per_sm = 1;
+        const long long needed = (work + groups_per_block - 1) / groups_per_block;
+        const unsigned blocks = static_cast<unsigned>(
+            std::max<long long>(1, std::min<long long>(needed, static_cast<long long>(sms) * per_sm)));
+        spai_columns_kernel<T, G, FAST><<<blocks, threads, smem, st>>>(args, mode, ws, qcap, nullptr);
+    } else {
+        const unsigned blocks = static_cast<unsigned>((work + groups_per_block - 1) / groups_per_block);
+        spai_columns_kernel<T, G, FAST><<<blocks, threads, 0, st>>>(args, 3, ws, qcap, gws);
+    }
+    SPAI_LAUNCH("spai_columns_kernel");
+}
+template <class T, bool FAST>
+void launch_columns_f(int G, ColumnArgs<T> args, int mode, size_t ws, int qcap, char *gws, size_t smem,
+                      int threads, long long work, int groups_per_block, int sms, cudaStream_t st) {
+    switch (G) {
+    case 4:
+        launch_columns_g<T, 4, FAST>(args, mode, ws, qcap, gws, smem, threads, work, groups_per_block, sms, st);
+        break;
+    case 8:
+        launch_columns_g<T, 8, FAST>(args, mode, ws, qcap, gws, smem, threads, work, groups_per_block, sms, st);
+        break;
+    case 16:
+        launch_columns_g<T, 16, FAST>(args, mode, ws, qcap, gws, smem, threads, work, groups_per_block, sms, st);
+        break;
+    default:
+        launch_columns_g<T, 32, FAST>(args, mode, ws, qcap, gws, smem, threads, work, groups_per_block, sms, st);
+    }
+}
+template <class T>
+void launch_columns(bool fast, int G, ColumnArgs<T> args, int mode, size_t ws, int qcap, char *gws,
+                    size_t smem, int threads, long long work, int groups_per_block, int sms,
+                    cudaStream_t st) {
+    if (fast)
+        launch_columns_f<T, true>(G, args, mode, ws, qcap, gws, smem, threads, work, groups_per_block, sms, st);
+    else
+        launch_columns_f<T, false>(G, args, mode, ws, qcap, gws, smem, threads, work, groups_per_block, sms, st);
+}
+
 template <class T>
 void SpaiBuilder<T>::construct(const DeviceCsr<T> &a, const SpaiParams &prm, cudaStream_t st,
                                SpaiOutput<T> &out, DeviceArena &arena) {
@@ -823,54 +1020,74 @@ void SpaiBuilder<T>::construct(const DeviceCsr<T> &a, const SpaiParams &prm, cud
     out.col_q = arena.alloc<int>(n);
     out.col_residual = arena.alloc<T>(n);
     long long *off = arena.alloc<long long>(n);
-    int *queue = arena.alloc<int>(4);
+    int *queue = arena.alloc<int>(8);
     int *err = arena.alloc<int>(1);
     unsigned long long *top = arena.alloc<unsigned long long>(1);
     int *ovl = arena.alloc<int>(n);
+    int *ovl2 = arena.alloc<int>(n);
     unsigned long long cap = std::max<unsigned long long>(static_cast<unsigned long long>(n) * 24ull, 1ull << 16);
     int *pidx = nullptr;
     T *pv = nullptr;
-    int ws_bytes = prm.ws_bytes_per_warp > 0 ? prm.ws_bytes_per_warp
-                                             : (sizeof(T) == 8 ? 16384 : 8192);
-    const int warps = prm.warps_per_block > 0 ? prm.warps_per_block : (sizeof(T) == 8 ? 12 : 24);
+    // Autotuned defaults from the sparsity profile (row lengths bound the shadow and candidate
+    // sets): short-row matrices (stencils) use many small workspaces; heavy-tailed rows use
+    // fewer, larger ones. Overrides come from SpaiParams.
+    const bool heavy = a.max_row > 48 || static_cast<double>(nnz) > 12.0 * n;
+    const int G = prm.group_lanes > 0 ? prm.group_lanes : (heavy ? 16 : 8);
+    const int ws_default = heavy ? 28672 : (sizeof(T) == 8 ? 12288 : 6144);
+    const int ws_bytes = prm.ws_bytes_per_warp > 0 ? prm.ws_bytes_per_warp : ws_default;
+    const int per_warp = 32 / G;
+    const int smem_budget = 225 * 1024;
+    // Groups per block: fill one SM's shared memory, within the register budget of one block
+    // (124 registers/thread for binary64, 77 for binary32 -> at most 512 / 768 threads), in
+    // whole warps.
+    const int max_threads = sizeof(T) == 8 ? 512 : 768;
+    int groups = prm.warps_per_block > 0 ? prm.warps_per_block * per_warp : smem_budget / ws_bytes;
+    groups = std::min(groups, max_threads / G);
+    groups = std::max(per_warp, (groups / per_warp) * per_warp);
+    if (static_cast<long long>(groups) * ws_bytes > smem_budget)
+        throw ArgumentError("SPAI workspace per group too large for one block's shared memory");
+    const int threads = ((groups * G + 31) / 32) * 32;
+    const int groups_launched = threads / G;
     const int qcap_main = 64;
+    out.group_lanes = G;
+    out.ws_bytes = ws_bytes;
     for (int attempt = 0;; ++attempt) {
         pidx = arena.alloc<int>(cap);
         pv = arena.alloc<T>(cap);
-        SPAI_CUDA(cudaMemsetAsync(queue, 0, sizeof(int) * 4, st));
+        SPAI_CUDA(cudaMemsetAsync(queue, 0, sizeof(int) * 8, st));
         SPAI_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
         SPAI_CUDA(cudaMemsetAsync(top, 0, sizeof(unsigned long long), st));
         ColumnArgs<T> args{n, a.rp, a.ci, a.val, tp, ti, d, static_cast<T>(prm.epsilon), prm.alpha,
                            prm.beta, out.col_status, out.col_fits, out.col_growths, out.col_clamps,
-                           out.col_q, out.col_residual, off, pidx, pv, top, cap, queue, ovl, err};
-        const size_t smem = static_cast<size_t>(ws_bytes) * warps;
-        SPAI_CUDA(cudaFuncSetAttribute(spai_columns_kernel<T>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       static_cast<int>(smem)));
+                           out.col_q, out.col_residual, off, pidx, pv, top, cap, queue, ovl, ovl2, err};
+        const size_t smem = static_cast<size_t>(ws_bytes) * groups_launched;
         int sms = 0, dev = 0;
         SPAI_CUDA(cudaGetDevice(&dev));
         SPAI_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-        int per_sm = 0;
-        SPAI_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, spai_columns_kernel<T>,
-                                                                warps * 32, smem));
-        if (per_sm < 1)
-            per_sm = 1;
-        const long long blocks_needed = (static_cast<long long>(n) + warps - 1) / warps;
-        const unsigned blocks =
-            static_cast<unsigned>(std::max<long long>(1, std::min<long long>(blocks_needed, static_cast<long long>(sms) * per_sm)));
-        spai_columns_kernel<T><<<blocks, warps * 32, smem, st>>>(args, 0, ws_bytes, qcap_main, nullptr);
-        SPAI_LAUNCH("spai_columns_kernel(main)");
+        launch_columns<T>(prm.fast, G, args, 0, ws_bytes, qcap_main, nullptr, smem, threads, n, groups_launched,
+                          sms, st);
         ++out.launches;
-        int h_queue[4];
+        int h_queue[8];
         SPAI_CUDA(cudaMemcpyAsync(h_queue, queue, sizeof(h_queue), cudaMemcpyDeviceToHost, st));
         SPAI_CUDA(cudaStreamSynchronize(st));
         out.overflow_columns = h_queue[1];
         if (h_queue[1] > 0) {
-            const size_t gws_bytes = prm.overflow_ws_bytes > 0 ? prm.overflow_ws_bytes : (size_t(8) << 20);
-            const int ow = std::min(h_queue[1], 1024);
-            char *gws = arena.alloc<char>(gws_bytes * ow);
-            spai_columns_kernel<T><<<ow, 32, 0, st>>>(args, 1, gws_bytes, 8192, gws);
-            SPAI_LAUNCH("spai_columns_kernel(overflow)");
+            // Tier 2: one 32-lane group per block with the whole shared memory of an SM. Columns
+            // that still do not fit are listed again (queue[3]) for tier 3.
+            const size_t big = static_cast<size_t>(smem_budget);
+            launch_columns<T>(prm.fast, 32, args, 2, big, 1024, nullptr, big, 32, std::min(h_queue[1], sms), 1,
+                              sms, st);
+            ++out.launches;
+            SPAI_CUDA(cudaMemcpyAsync(h_queue, queue, sizeof(h_queue), cudaMemcpyDeviceToHost, st));
+            SPAI_CUDA(cudaStreamSynchronize(st));
+            out.overflow_columns_global = h_queue[3];
+        }
+        if (h_queue[3] > 0) {
+            // Tier 3: global-memory workspace per 32-lane group.
+            const size_t gws_bytes = prm.overflow_ws_bytes > 0 ? prm.overflow_ws_bytes : (size_t(32) << 20);
+            const int og = std::min(h_queue[3], 512);
+            char *gws = arena.alloc<char>(gws_bytes * og);
+            launch_columns<T>(prm.fast, 32, args, 3, gws_bytes, 65536, gws, 0, 32, og, 1, sms, st);
             ++out.launches;
         }
         int h_err = 0;

@@ -14,6 +14,7 @@ namespace spai {
 // Device CSR with 32-bit indices (nnz < 2^31 is checked at upload).
 template <class T> struct DeviceCsr {
     int n = 0, nnz = 0;
+    int max_row = 0; // longest row (sparsity profile for tuning)
     int *rp = nullptr, *ci = nullptr;
     T *val = nullptr;
 };
@@ -68,8 +69,10 @@ struct SpaiParams {
     double epsilon = 0.3;
     long long alpha = 5;
     int beta = 8;
-    int ws_bytes_per_warp = 0;   // 0 = tuned default
-    int warps_per_block = 0;     // 0 = tuned default
+    int ws_bytes_per_warp = 0;   // workspace per column group (bytes); 0 = tuned default
+    int warps_per_block = 0;     // 0 = fill the shared memory of one block per SM
+    int group_lanes = 0;         // lanes per column (4, 8, 16, 32); 0 = tuned default
+    bool fast = false;           // parallel norms/mean, hashed candidates (not bit-reproducing)
     size_t overflow_ws_bytes = 0;
 };
 
@@ -80,6 +83,8 @@ template <class T> struct SpaiOutput {
     long long fits = 0, growths = 0;
     int overflow_columns = 0;
     long long launches = 0;
+    int group_lanes = 0, ws_bytes = 0;
+    int overflow_columns_global = 0;
     T *d = nullptr;
     int *col_status = nullptr, *col_fits = nullptr, *col_growths = nullptr, *col_clamps = nullptr,
         *col_q = nullptr;

@@ -16,6 +16,8 @@ CLI_DIR = os.path.join(PKG, "_build")
 
 PRECISION = {"f64": 0, "f32": 1, "mixed": 2}
 FLAG_NO_GRAPH = 1
+FLAG_FAST_SPAI = 2
+FLAG_EXACT_SPAI = 0  # sequential, bit-reproducing SPAI (the default)
 
 SPAI_STATUS = ["success", "not_attempted", "invalid_input", "rank_deficient", "numerical_failure",
                "empty_candidates", "zero_denominator", "invalid_score", "no_growth", "iteration_limit"]
@@ -246,7 +248,7 @@ class Handle:
         """Allocation-free backward error of device vector x (see spai_backward_error_noalloc)."""
         _check(lib().spai_backward_error_noalloc(self._h, VP(d_b), VP(d_x), VP(d_out), stream))
 
-    KERNEL_CLASSES = ("spmv_A", "spmv_P", "cgs_dots", "cgs_update", "normalize")
+    KERNEL_CLASSES = ("spmv_A", "spmv_P", "cgs_pass1", "cgs_pass2", "cgs_pass3")
 
     def profile(self, enable=True):
         _check(lib().spai_profile(self._h, 1 if enable else 0))
