@@ -184,8 +184,14 @@ int spai_gmres(spai_handle *h, const double *rhs, double *x, double tau, int64_t
 /* Score guard KAT on the device (cuda_evaluate_spai_score). out = {status, score, clamped}. */
 int spai_score(int32_t precision, double rsq, double dot, double den, double *out);
 
-/* Batched: `count` independent systems, each with its own SPAI, solved together (one build pass
- * and one refinement loop over all systems). b[i], x[i] are host vectors of systems[i].n. */
+/* Batched: `count` independent systems of any sizes, each with its own SPAI, in the mixed form
+ * (opt->precision must be SPAI_PREC_MIXED, else SPAI_ERR_UNSUPPORTED). One SPAI build over the
+ * block-diagonal union (identical to each system's own SPAI), then one persistent launch in which
+ * each CTA runs one system's whole refinement. b[i], x[i] are host vectors of systems[i].n;
+ * reports[i] is system i's IrResult summary (spai_ms/solve_ms are the whole batch's). Failures
+ * stay per system (invalid_input, construction_failure). innercap = 0 means cap = n per system;
+ * caps above 1936 are rejected (per-CTA Hessenberg workspace). No reference counterpart (the
+ * reference solves one system per call). */
 int spai_ir_solve_batched(int64_t count, const spai_csr *systems, const double *const *b,
                           double *const *x, const spai_options *opt, spai_report *reports,
                           void *stream);
@@ -195,6 +201,14 @@ int spai_ir_solve_batched(int64_t count, const spai_csr *systems, const double *
  * dLdb = lambda and dLdA[e] = -sum_r lambda_r[i] x_r[j] over A's pattern (e = (i, j)). */
 int spai_adjoint(spai_handle *h, int64_t nrhs, const double *x, const double *dLdx,
                  double *dLdb, double *dLdA_values, const spai_options *opt, spai_report *rep);
+/* Same with device pointers (stream-ordered on the handle's stream, synchronous on return). The
+ * report aggregates the nrhs solves: converged iff all converged, the first failing status,
+ * the largest backward error, summed inner iterations and device time. dLdA follows the order
+ * of the stored entries of the CSR given to spai_create. No reference counterpart (the
+ * reference has no adjoint). */
+int spai_adjoint_device(spai_handle *h, int64_t nrhs, const double *d_x, const double *d_dLdx,
+                        double *d_dLdb, double *d_dLdA_values, const spai_options *opt,
+                        spai_report *rep);
 
 /* Per-kernel-class timing of refinement solves (CUDA events on the handle's stream around each
  * launch). Classes: 0 SpMV with A (basis vector gathered), 1 SpMV with P, 2 Gram-Schmidt pass 1

@@ -1,5 +1,6 @@
 // C ABI of libspai_ir.so: handle management, uploads, SPAI build, refinement solves.
 // The entry points and their reference counterparts are listed in include/spai_ir.h.
+#include "adjoint.cuh"
 #include "krylov_kernels.cuh"
 #include "spai_ir.h"
 
@@ -110,6 +111,16 @@ struct spai_handle_s {
     IrEngine<float, double> emix;
     IrEngine<float, float> e32;
     int engine_cap = -1;
+    // Adjoint solves A^T lambda = g: transposes of A and P built on first use after a build, and
+    // engines in right-preconditioned mode over them.
+    DeviceArena adj, adj_solve, conv;
+    DeviceCsr<double> at64, pt64;
+    DeviceCsr<float> at32, pt32;
+    bool adj_ready = false;
+    IrEngine<double, double> j64;
+    IrEngine<float, double> jmix;
+    IrEngine<float, float> j32;
+    int adj_cap = -1;
     KernelProfile prof;
     double spai_ms = 0;
     long long spai_launches = 0;
@@ -214,6 +225,82 @@ bool options_valid(const spai_handle *h, const spai_options &o) {
            std::isfinite(inner_tau(o)) && inner_tau(o) > 0 && o.alpha >= 0 && o.beta >= 0;
 }
 
+// Build the transposes of A and P once per build, and the right-preconditioned engines for `cap`.
+void ensure_adjoint(spai_handle *h, int cap) {
+    cudaStream_t st = h->stream;
+    if (!h->adj_ready) {
+        h->adj.reset();
+        const TransposePlan ta = transpose_plan(h->adj, h->a64, h->sms, st);
+        h->at64 = transpose_values(h->adj, ta, h->a64.val, h->sms, st);
+        if (h->inner_f32()) {
+            h->at32 = transpose_values(h->adj, ta, h->a32.val, h->sms, st);
+            const TransposePlan tp = transpose_plan(h->adj, h->s32.p, h->sms, st);
+            h->pt32 = transpose_values(h->adj, tp, h->s32.p.val, h->sms, st);
+        } else {
+            const TransposePlan tp = transpose_plan(h->adj, h->s64.p, h->sms, st);
+            h->pt64 = transpose_values(h->adj, tp, h->s64.p.val, h->sms, st);
+        }
+        SPAI_CUDA(cudaStreamSynchronize(st));
+        h->adj_ready = true;
+        h->adj_cap = -1;
+    }
+    if (h->adj_cap == cap)
+        return;
+    h->adj_solve.reset();
+    if (h->precision == SPAI_PREC_F64)
+        h->j64.setup(h->adj_solve, h->at64, h->at64, h->pt64, cap, h->sms, true);
+    else if (h->precision == SPAI_PREC_MIXED)
+        h->jmix.setup(h->adj_solve, h->at64, h->at32, h->pt32, cap, h->sms, true);
+    else
+        h->j32.setup(h->adj_solve, h->at32, h->at32, h->pt32, cap, h->sms, true);
+    h->adj_cap = cap;
+}
+
+// One refinement solve on the engine of the handle's precision; b, x device binary64 vectors.
+template <class E64, class EMX, class E32>
+void run_solve(spai_handle *h, E64 &e64, EMX &emix, E32 &e32, const double *d_b, double *d_x,
+               const SolveSettings &s, spai_report *rep) {
+    EventTimer timer(h->stream);
+    Ctl c{};
+    if (h->precision == SPAI_PREC_F64) {
+        e64.solve(h->stream, d_b, d_x, s, h->pinned);
+        rep->solve_ms = timer.stop();
+        read_ctl(h, e64, c);
+        rep->kernel_launches = e64.graph_mode ? e64.graph_kernels(c) : e64.launches;
+    } else if (h->precision == SPAI_PREC_MIXED) {
+        emix.solve(h->stream, d_b, d_x, s, h->pinned);
+        rep->solve_ms = timer.stop();
+        read_ctl(h, emix, c);
+        rep->kernel_launches = emix.graph_mode ? emix.graph_kernels(c) : emix.launches;
+    } else {
+        // binary32 drop-in: b rounded to binary32, refinement in binary32.
+        h->conv.reset();
+        float *bf = h->conv.alloc<float>(h->n);
+        float *xf = h->conv.alloc<float>(h->n);
+        convert_kernel<float, double><<<grid_for(h->n, 256, h->sms * 8), 256, 0, h->stream>>>(h->n, d_b, bf);
+        SPAI_LAUNCH("convert_kernel");
+        e32.solve(h->stream, bf, xf, s, h->pinned);
+        convert_kernel<double, float><<<grid_for(h->n, 256, h->sms * 8), 256, 0, h->stream>>>(h->n, xf, d_x);
+        SPAI_LAUNCH("convert_kernel");
+        rep->solve_ms = timer.stop();
+        read_ctl(h, e32, c);
+        rep->kernel_launches = (e32.graph_mode ? e32.graph_kernels(c) : e32.launches) + 2;
+    }
+    fill_from_ctl(c, rep);
+}
+
+SolveSettings settings_for(const spai_handle *h, const spai_options &o, int cap) {
+    SolveSettings s;
+    s.cap = cap;
+    s.outer_cap = static_cast<int>(o.outercap);
+    s.tau = inner_tau(o);
+    s.be_tol = be_tol(o);
+    s.scale_rhs = h->precision == SPAI_PREC_MIXED;
+    s.accept_every = h->precision == SPAI_PREC_F32;
+    s.use_graph = (o.flags & SPAI_FLAG_NO_GRAPH) == 0;
+    return s;
+}
+
 // Solve with device vectors b, x (binary64). Returns SPAI_OK and fills rep.
 int solve_device_impl(spai_handle *h, const double *d_b, double *d_x, const spai_options &o,
                       spai_report *rep) {
@@ -231,42 +318,70 @@ int solve_device_impl(spai_handle *h, const double *d_b, double *d_x, const spai
     }
     const int cap = o.innercap == 0 ? h->n : static_cast<int>(o.innercap);
     ensure_engine(h, cap);
-    SolveSettings s;
-    s.cap = cap;
-    s.outer_cap = static_cast<int>(o.outercap);
-    s.tau = inner_tau(o);
-    s.be_tol = be_tol(o);
-    s.scale_rhs = h->precision == SPAI_PREC_MIXED;
-    s.accept_every = h->precision == SPAI_PREC_F32;
-    s.use_graph = (o.flags & SPAI_FLAG_NO_GRAPH) == 0;
-    EventTimer timer(h->stream);
-    Ctl c{};
-    if (h->precision == SPAI_PREC_F64) {
-        h->e64.solve(h->stream, d_b, d_x, s, h->pinned);
-        rep->solve_ms = timer.stop();
-        read_ctl(h, h->e64, c);
-        rep->kernel_launches = h->e64.graph_mode ? h->e64.graph_kernels(c) : h->e64.launches;
-    } else if (h->precision == SPAI_PREC_MIXED) {
-        h->emix.solve(h->stream, d_b, d_x, s, h->pinned);
-        rep->solve_ms = timer.stop();
-        read_ctl(h, h->emix, c);
-        rep->kernel_launches = h->emix.graph_mode ? h->emix.graph_kernels(c) : h->emix.launches;
-    } else {
-        // binary32 drop-in: b rounded to binary32, refinement in binary32.
-        h->scratch.reset();
-        float *bf = h->scratch.alloc<float>(h->n);
-        float *xf = h->scratch.alloc<float>(h->n);
-        convert_kernel<float, double><<<grid_for(h->n, 256, h->sms * 8), 256, 0, h->stream>>>(h->n, d_b, bf);
-        SPAI_LAUNCH("convert_kernel");
-        h->e32.solve(h->stream, bf, xf, s, h->pinned);
-        convert_kernel<double, float><<<grid_for(h->n, 256, h->sms * 8), 256, 0, h->stream>>>(h->n, xf, d_x);
-        SPAI_LAUNCH("convert_kernel");
-        rep->solve_ms = timer.stop();
-        read_ctl(h, h->e32, c);
-        rep->kernel_launches = (h->e32.graph_mode ? h->e32.graph_kernels(c) : h->e32.launches) + 2;
-    }
-    fill_from_ctl(c, rep);
+    run_solve(h, h->e64, h->emix, h->e32, d_b, d_x, settings_for(h, o, cap), rep);
     rep->nnz_p = h->precision == SPAI_PREC_F64 ? h->s64.p.nnz : h->s32.p.nnz;
+    return SPAI_OK;
+}
+
+// Adjoint of x_r = A^{-1} b_r for r < nrhs (device, column-major n x nrhs): lambda_r solves
+// A^T lambda_r = g_r by refinement whose inner GMRES is right-preconditioned with P^T; then
+// dLdb = lambda and dLdA[e] = -sum_r lambda_r[i] x_r[j]. The report aggregates the solves:
+// converged iff all converged, the first non-success status, the largest backward error and
+// outer step count, summed inner iterations, launches and solve time.
+int adjoint_device_impl(spai_handle *h, int nrhs, const double *d_x, const double *d_g, double *d_lambda,
+                        double *d_dlda, const spai_options &o, spai_report *rep) {
+    if (!h->built)
+        return fail(SPAI_ERR_NOT_BUILT, "spai_adjoint before a successful spai_build");
+    rep->spai_status = h->spai_status;
+    rep->spai_ms = h->spai_ms;
+    if (h->spai_status != SPAI_SUCCESS) {
+        rep->ir_status = IR_CONSTRUCTION_FAILURE;
+        return SPAI_OK;
+    }
+    if (!options_valid(h, o)) {
+        rep->ir_status = IR_INVALID_INPUT;
+        return SPAI_OK;
+    }
+    const int n = h->n;
+    const int cap = o.innercap == 0 ? n : static_cast<int>(o.innercap);
+    ensure_adjoint(h, cap);
+    const SolveSettings s = settings_for(h, o, cap);
+    spai_report agg = *rep;
+    agg.ir_status = IR_SUCCESS;
+    agg.converged = 1;
+    agg.backward_error = 0;
+    agg.componentwise_backward_error = 0;
+    agg.residual_inf = 0;
+    agg.solve_ms = 0;
+    agg.kernel_launches = 0;
+    for (int r = 0; r < nrhs; ++r) {
+        const size_t off = static_cast<size_t>(r) * n;
+        spai_report one = *rep;
+        run_solve(h, h->j64, h->jmix, h->j32, d_g + off, d_lambda + off, s, &one);
+        if (!one.converged && agg.converged) {
+            agg.converged = 0;
+            agg.ir_status = one.ir_status;
+            agg.gmres_status = one.gmres_status;
+        }
+        if (agg.converged)
+            agg.gmres_status = one.gmres_status;
+        agg.outer_steps = std::max(agg.outer_steps, one.outer_steps);
+        agg.inner_attempts += one.inner_attempts;
+        agg.inner_iterations += one.inner_iterations;
+        agg.backward_error = std::max(agg.backward_error, one.backward_error);
+        agg.componentwise_backward_error = std::max(agg.componentwise_backward_error, one.componentwise_backward_error);
+        agg.residual_inf = std::max(agg.residual_inf, one.residual_inf);
+        agg.solve_ms += one.solve_ms;
+        agg.kernel_launches += one.kernel_launches;
+    }
+    EventTimer timer(h->stream);
+    sampled_outer_kernel<<<grid_for(n, 256, h->sms * 8), 256, 0, h->stream>>>(n, nrhs, h->a64.rp, h->a64.ci,
+                                                                           d_lambda, d_x, d_dlda);
+    SPAI_LAUNCH("sampled_outer_kernel");
+    agg.solve_ms += timer.stop();
+    agg.kernel_launches += 1;
+    agg.nnz_p = h->precision == SPAI_PREC_F64 ? h->s64.p.nnz : h->s32.p.nnz;
+    *rep = agg;
     return SPAI_OK;
 }
 
@@ -398,6 +513,8 @@ int spai_build(spai_handle *h, const spai_options *opt, spai_report *rep) {
     SPAI_CUDA(cudaSetDevice(h->device));
     h->built = false;
     h->engine_cap = -1;
+    h->adj_ready = false;
+    h->adj_cap = -1;
     h->build.reset();
     SpaiParams prm;
     // Tuning overrides (group width, per-group workspace) for profiling sweeps.
@@ -802,30 +919,54 @@ int spai_profile_read(spai_handle *h, int32_t cls, double *ms, int64_t *launches
     API_END
 }
 
-int spai_ir_solve_batched(int64_t count, const spai_csr *systems, const double *const *b,
-                          double *const *x, const spai_options *opt, spai_report *reports,
-                          void *stream) {
-    (void)count;
-    (void)systems;
-    (void)b;
-    (void)x;
-    (void)opt;
-    (void)reports;
-    (void)stream;
-    return fail(SPAI_ERR_UNSUPPORTED, "spai_ir_solve_batched: not built yet");
+int spai_adjoint_device(spai_handle *h, int64_t nrhs, const double *d_x, const double *d_dLdx,
+                        double *d_dLdb, double *d_dLdA_values, const spai_options *opt, spai_report *rep) {
+    API_BEGIN
+    if (!h || !opt || nrhs < 1 || nrhs > INT_MAX || !d_x || !d_dLdx || !d_dLdb || !d_dLdA_values)
+        return fail(SPAI_ERR_ARGUMENT, "spai_adjoint_device: bad arguments");
+    spai_report local;
+    if (!rep)
+        rep = &local;
+    clear_report(rep);
+    SPAI_CUDA(cudaSetDevice(h->device));
+    return adjoint_device_impl(h, static_cast<int>(nrhs), d_x, d_dLdx, d_dLdb, d_dLdA_values, *opt, rep);
+    API_END
 }
 
 int spai_adjoint(spai_handle *h, int64_t nrhs, const double *x, const double *dLdx, double *dLdb,
                  double *dLdA_values, const spai_options *opt, spai_report *rep) {
-    (void)h;
-    (void)nrhs;
-    (void)x;
-    (void)dLdx;
-    (void)dLdb;
-    (void)dLdA_values;
-    (void)opt;
-    (void)rep;
-    return fail(SPAI_ERR_UNSUPPORTED, "spai_adjoint: not built yet");
+    API_BEGIN
+    if (!h || !opt || nrhs < 1 || nrhs > INT_MAX || !x || !dLdx || !dLdb || !dLdA_values)
+        return fail(SPAI_ERR_ARGUMENT, "spai_adjoint: bad arguments");
+    spai_report local;
+    if (!rep)
+        rep = &local;
+    clear_report(rep);
+    SPAI_CUDA(cudaSetDevice(h->device));
+    const size_t total = static_cast<size_t>(nrhs) * h->n;
+    for (size_t i = 0; i < total; ++i)
+        if (!std::isfinite(x[i]) || !std::isfinite(dLdx[i])) {
+            rep->ir_status = IR_INVALID_INPUT;
+            rep->spai_status = h->spai_status;
+            return SPAI_OK;
+        }
+    h->scratch.reset();
+    double *dx = h->scratch.alloc<double>(total);
+    double *dg = h->scratch.alloc<double>(total);
+    double *dl = h->scratch.alloc<double>(total);
+    double *da = h->scratch.alloc<double>(h->nnz);
+    SPAI_CUDA(cudaMemcpyAsync(dx, x, sizeof(double) * total, cudaMemcpyHostToDevice, h->stream));
+    SPAI_CUDA(cudaMemcpyAsync(dg, dLdx, sizeof(double) * total, cudaMemcpyHostToDevice, h->stream));
+    const int rc = adjoint_device_impl(h, static_cast<int>(nrhs), dx, dg, dl, da, *opt, rep);
+    if (rc != SPAI_OK)
+        return rc;
+    if (rep->ir_status != IR_CONSTRUCTION_FAILURE && rep->ir_status != IR_INVALID_INPUT) {
+        SPAI_CUDA(cudaMemcpyAsync(dLdb, dl, sizeof(double) * total, cudaMemcpyDeviceToHost, h->stream));
+        SPAI_CUDA(cudaMemcpyAsync(dLdA_values, da, sizeof(double) * h->nnz, cudaMemcpyDeviceToHost, h->stream));
+        SPAI_CUDA(cudaStreamSynchronize(h->stream));
+    }
+    return SPAI_OK;
+    API_END
 }
 
 } // extern "C"

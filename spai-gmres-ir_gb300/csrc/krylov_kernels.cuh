@@ -204,22 +204,52 @@ __global__ void __launch_bounds__(kBlock) norm_kernel(int n, VecRef<T> ar, const
 } // namespace kdetail
 
 // Back substitution y = R^{-1} g over `count` columns (src/gmres.cpp:47-55); count = k+1, or k
-// when the zero-pivot branch re-verifies the previous candidate. One block.
+// when the zero-pivot branch re-verifies the previous candidate. One block, blocked by 32 columns
+// from the bottom: warp 0 solves the 32 x 32 diagonal block (lane per row, column sweep), then
+// every thread removes the block's contribution from the rows above it (coalesced over R's
+// column-major storage). O(count / 32) barriers instead of an O(count^2) serial loop; this runs
+// at every step once the recursive estimate has dropped below tau on systems whose recomputed
+// residual stays above it.
 template <class T>
-__global__ void solve_y_kernel(Ctl *ctl, const T *H, int hld, const T *g, T *y) {
+__global__ void __launch_bounds__(256) solve_y_kernel(Ctl *ctl, const T *H, int hld, const T *g, T *y) {
     if (!ctl->active || !ctl->vgate)
         return;
     const int k = ctl->k;
     const int count = ctl->triggered == 2 ? k : k + 1;
-    if (threadIdx.x == 0) {
-        bool bad = false;
-        for (int r = count - 1; r >= 0; --r) {
-            T v = g[r];
-            for (int c = r + 1; c < count; ++c)
-                v -= H[static_cast<long long>(c) * hld + r] * y[c];
-            y[r] = v / H[static_cast<long long>(r) * hld + r];
-            bad |= !isfinite(y[r]);
+    for (int r = threadIdx.x; r < count; r += blockDim.x)
+        y[r] = g[r];
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int bad = 0;
+    for (int hi = count; hi > 0; hi -= 32) {
+        const int lo = hi > 32 ? hi - 32 : 0;
+        if (warp == 0) {
+            const int row = lo + lane;
+            T yr = row < hi ? y[row] : T(0);
+            for (int c = hi - 1; c >= lo; --c) {
+                const T *hc = H + static_cast<long long>(c) * hld;
+                const T yc = __shfl_sync(0xffffffffu, yr, c - lo) / hc[c];
+                if (row == c)
+                    yr = yc;
+                else if (row < c)
+                    yr -= hc[row] * yc;
+            }
+            if (row < hi) {
+                y[row] = yr;
+                bad |= !isfinite(yr);
+            }
         }
+        __syncthreads();
+        for (int r = threadIdx.x; r < lo; r += blockDim.x) {
+            T acc = 0;
+            for (int c = lo; c < hi; ++c)
+                acc += H[static_cast<long long>(c) * hld + r] * y[c];
+            y[r] -= acc;
+        }
+        __syncthreads();
+    }
+    bad = __syncthreads_or(bad);
+    if (threadIdx.x == 0) {
         ctl->formed = count;
         if (bad) {
             ctl->status = 8;
@@ -697,13 +727,18 @@ template <class T, class TO> struct IrEngine {
     cudaGraphExec_t exec = nullptr;
     bool graph_f32_accept = false;
     bool graph_mode = false;
+    // Right preconditioning (adjoint solves): the operator is (inner matrix)·P, GMRES starts from
+    // rhs itself, the candidate is d = P·(V y) and its only check is the true residual.
+    bool right = false;
 
     // Kernel nodes executed by the last graph solve, from the device loop counters: 4 init
-    // nodes; per GMRES solve 8 start nodes and 6 update/residual nodes; per Arnoldi step 7 passes,
-    // 2 condition sets and the decision; per candidate verification 6.
+    // nodes; per GMRES solve 8 start nodes (7 with right preconditioning) and 6 update/residual
+    // nodes; per Arnoldi step 7 passes, 2 condition sets and the decision; per candidate
+    // verification 6 (5 with right preconditioning).
     long long graph_kernels(const Ctl &c) const {
         const long long steps = static_cast<long long>(c.guard) + c.inner_attempts;
-        return 4 + 14LL * c.inner_attempts + 10LL * steps + 6LL * c.verifications;
+        return 4 + (right ? 13LL : 14LL) * c.inner_attempts + 10LL * steps +
+               (right ? 5LL : 6LL) * c.verifications;
     }
 
     ~IrEngine() {
@@ -784,7 +819,7 @@ template <class T, class TO> struct IrEngine {
         const auto n_verify = add_conditional(body_inner, e1, h_verify, cudaGraphCondTypeIf, &body_verify);
         capture_into(st, body_verify, {}, [&] { verify_checks(st); });
         capture_into(st, body_inner, {n_verify}, [&] {
-            decide_kernel<T><<<1, 32, 0, st>>>(ctl, scal + 0, scal + 1);
+            decide_kernel<T><<<1, 32, 0, st>>>(ctl, scal + 0, relnum());
             set_cond_kernel<<<1, 32, 0, st>>>(h_inner, &ctl->active);
         });
         capture_into(st, body_outer, {n_inner}, [&] {
@@ -812,7 +847,8 @@ template <class T, class TO> struct IrEngine {
     }
 
     void setup(DeviceArena &arena, const DeviceCsr<TO> &ao, const DeviceCsr<T> &ai,
-               const DeviceCsr<T> &pp, int cap_, int sms_) {
+               const DeviceCsr<T> &pp, int cap_, int sms_, bool right_ = false) {
+        right = right_;
         a_outer = &ao;
         a_inner = &ai;
         p = &pp;
@@ -901,16 +937,27 @@ template <class T, class TO> struct IrEngine {
         ++host_k;
     }
 
+    // Vector the candidate check compares with (P·rhs, or rhs itself with right preconditioning)
+    // and the numerator of the relative residual the decision uses.
+    const T *pbv() const {
+        return right ? rhs : pb;
+    }
+    const T *relnum() const {
+        return right ? scal + 0 : scal + 1;
+    }
+
     void arnoldi_passes(cudaStream_t st) {
         const double kk = host_k;
-        timed(st, kClsSpmvA, spmv_bytes(*a_inner), [&] {
-            const int G = pick_group(*a_inner);
+        // w = P·(A v) (left) or w = A·(P v) (right): the first matrix gathers the basis vector.
+        const DeviceCsr<T> &m1 = right ? *p : *a_inner;
+        const DeviceCsr<T> &m2 = right ? *a_inner : *p;
+        timed(st, kClsSpmvA, spmv_bytes(m1), [&] {
+            const int G = pick_group(m1);
             const unsigned blocks = grid_for(static_cast<long long>(n) * G, 256, sms * 16);
             const Basis<T> vb = basis();
 #define SPAI_SPMV_BASIS(g)                                                                         \
     case g:                                                                                        \
-        spmv_basis_kernel<T, g><<<blocks, 256, 0, st>>>(n, a_inner->rp, a_inner->ci, a_inner->val, \
-                                                        vb, t, ctl);                               \
+        spmv_basis_kernel<T, g><<<blocks, 256, 0, st>>>(n, m1.rp, m1.ci, m1.val, vb, t, ctl);      \
         break;
             switch (G) {
                 SPAI_SPMV_BASIS(2)
@@ -922,8 +969,8 @@ template <class T, class TO> struct IrEngine {
 #undef SPAI_SPMV_BASIS
             SPAI_LAUNCH("spmv_basis_kernel");
         });
-        timed(st, kClsSpmvP, spmv_bytes(*p), [&] {
-            launch_spmv<T, T, T>(*p, fixed(t), fixed(w), &ctl->active, sms, st);
+        timed(st, kClsSpmvP, spmv_bytes(m2), [&] {
+            launch_spmv<T, T, T>(m2, fixed(t), fixed(w), &ctl->active, sms, st);
         });
         const size_t smem = cgs_smem();
         const CgsArgs<T> args = cgs_args();
@@ -952,17 +999,28 @@ template <class T, class TO> struct IrEngine {
 
     void verify(cudaStream_t st) {
         verify_checks(st);
-        decide_kernel<T><<<1, 32, 0, st>>>(ctl, scal + 0, scal + 1);
+        decide_kernel<T><<<1, 32, 0, st>>>(ctl, scal + 0, relnum());
         SPAI_LAUNCH("decide_kernel");
         ++launches;
     }
 
     void verify_checks(cudaStream_t st) {
-        solve_y_kernel<T><<<1, 32, 0, st>>>(ctl, H, hld, g, y);
+        solve_y_kernel<T><<<1, 256, 0, st>>>(ctl, H, hld, g, y);
         SPAI_LAUNCH("solve_y_kernel");
+        const int *g2 = &ctl->vgate;
+        if (right) {
+            // d = P·(V y); recomputed residual ||rhs - A d|| (right preconditioning leaves the
+            // residual unpreconditioned, so it is also the decision's numerator).
+            form_candidate_tiles_kernel<T><<<nblk_vec, kBlock, 0, st>>>(n, basis(), y, pax, ctl);
+            SPAI_LAUNCH("form_candidate_tiles_kernel");
+            launch_spmv<T, T, T>(*p, fixed(pax), fixed(cand), g2, sms, st);
+            launch_spmv<T, T, T>(*a_inner, fixed(cand), fixed(ax), g2, sms, st);
+            norm(st, fixed(rhs), ax, scal + 0, kSlotNormA, g2);
+            launches += 3;
+            return;
+        }
         form_candidate_tiles_kernel<T><<<nblk_vec, kBlock, 0, st>>>(n, basis(), y, cand, ctl);
         SPAI_LAUNCH("form_candidate_tiles_kernel");
-        const int *g2 = &ctl->vgate;
         launch_spmv<T, T, T>(*a_inner, fixed(cand), fixed(ax), g2, sms, st);
         norm(st, fixed(rhs), ax, scal + 0, kSlotNormA, g2);
         launch_spmv<T, T, T>(*p, fixed(ax), fixed(pax), g2, sms, st);
@@ -970,18 +1028,22 @@ template <class T, class TO> struct IrEngine {
         launches += 4;
     }
 
-    // GMRES start for the current rhs (x0 = 0): ||rhs||, Pb, ||Pb||, v0 = Pb/||Pb||.
+    // GMRES start for the current rhs (x0 = 0): ||rhs||, Pb, ||Pb||, v0 = Pb/||Pb||; with right
+    // preconditioning v0 = rhs/||rhs|| and the estimate is relative to ||rhs||.
     void gmres_start(cudaStream_t st, bool accept_every) {
         norm(st, fixed(rhs), nullptr, scal + 2, kSlotNormA, &ctl->outer_active);
         gmres_start_kernel<T><<<1, 32, 0, st>>>(ctl, scal + 2, accept_every ? 1 : 0);
         SPAI_LAUNCH("gmres_start_kernel");
-        launch_spmv<T, T, T>(*p, fixed(rhs), fixed(pb), &ctl->active, sms, st);
-        norm(st, fixed(pb), nullptr, scal + 3, kSlotNormB, &ctl->active);
+        if (!right) {
+            launch_spmv<T, T, T>(*p, fixed(rhs), fixed(pb), &ctl->active, sms, st);
+            ++launches;
+        }
+        norm(st, fixed(const_cast<T *>(pbv())), nullptr, scal + 3, kSlotNormB, &ctl->active);
         gmres_den_kernel<T><<<1, 32, 0, st>>>(ctl, scal + 3, g, accept_every ? 1 : 0);
         SPAI_LAUNCH("gmres_den_kernel");
-        basis_start_kernel<T><<<nblk_vec, kBlock, 0, st>>>(n, basis(), pb, sc, ctl);
+        basis_start_kernel<T><<<nblk_vec, kBlock, 0, st>>>(n, basis(), pbv(), sc, ctl);
         SPAI_LAUNCH("basis_start_kernel");
-        launches += 4;
+        launches += 3;
     }
 
     int read_flag(cudaStream_t st, int *host_flag, const int *dev_flag) {

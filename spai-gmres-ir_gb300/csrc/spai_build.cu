@@ -21,6 +21,10 @@
 #include <cooperative_groups.h>
 #include <cub/device/device_scan.cuh>
 
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
+
 #include <algorithm>
 #include <vector>
 
@@ -1051,6 +1055,12 @@ void SpaiBuilder<T>::construct(const DeviceCsr<T> &a, const SpaiParams &prm, cud
     const int qcap_main = 64;
     out.group_lanes = G;
     out.ws_bytes = ws_bytes;
+    // SPAI_TRACE=1 prints the wall time of each workspace tier to stderr (tuning aid).
+    const bool trace = std::getenv("SPAI_TRACE") != nullptr;
+    auto clock_ms = [] {
+        return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
+    };
+    double t_tier = clock_ms();
     for (int attempt = 0;; ++attempt) {
         pidx = arena.alloc<int>(cap);
         pv = arena.alloc<T>(cap);
@@ -1071,6 +1081,11 @@ void SpaiBuilder<T>::construct(const DeviceCsr<T> &a, const SpaiParams &prm, cud
         SPAI_CUDA(cudaMemcpyAsync(h_queue, queue, sizeof(h_queue), cudaMemcpyDeviceToHost, st));
         SPAI_CUDA(cudaStreamSynchronize(st));
         out.overflow_columns = h_queue[1];
+        if (trace) {
+            std::fprintf(stderr, "spai main tier: G=%d ws=%d groups/block=%d  %.1f ms, overflow %d\n", G, ws_bytes,
+                         groups_launched, clock_ms() - t_tier, h_queue[1]);
+            t_tier = clock_ms();
+        }
         if (h_queue[1] > 0) {
             // Tier 2: one 32-lane group per block with the whole shared memory of an SM. Columns
             // that still do not fit are listed again (queue[3]) for tier 3.
@@ -1081,6 +1096,10 @@ void SpaiBuilder<T>::construct(const DeviceCsr<T> &a, const SpaiParams &prm, cud
             SPAI_CUDA(cudaMemcpyAsync(h_queue, queue, sizeof(h_queue), cudaMemcpyDeviceToHost, st));
             SPAI_CUDA(cudaStreamSynchronize(st));
             out.overflow_columns_global = h_queue[3];
+            if (trace) {
+                std::fprintf(stderr, "spai shared tier: %.1f ms, to global %d\n", clock_ms() - t_tier, h_queue[3]);
+                t_tier = clock_ms();
+            }
         }
         if (h_queue[3] > 0) {
             // Tier 3: global-memory workspace per 32-lane group.
@@ -1089,6 +1108,10 @@ void SpaiBuilder<T>::construct(const DeviceCsr<T> &a, const SpaiParams &prm, cud
             char *gws = arena.alloc<char>(gws_bytes * og);
             launch_columns<T>(prm.fast, 32, args, 3, gws_bytes, 65536, gws, 0, 32, og, 1, sms, st);
             ++out.launches;
+            if (trace) {
+                SPAI_CUDA(cudaStreamSynchronize(st));
+                std::fprintf(stderr, "spai global tier: %.1f ms (%d groups)\n", clock_ms() - t_tier, og);
+            }
         }
         int h_err = 0;
         SPAI_CUDA(cudaMemcpyAsync(&h_err, err, sizeof(int), cudaMemcpyDeviceToHost, st));

@@ -27,6 +27,9 @@ GMRES_STATUS = ["success", "zero_rhs", "exact_initial_solution", "invalid_input"
 IR_STATUS = ["success", "invalid_input", "construction_failure", "inner_failure", "stagnation",
              "iteration_limit", "numerical_failure"]
 
+(IR_SUCCESS, IR_INVALID_INPUT, IR_CONSTRUCTION_FAILURE, IR_INNER_FAILURE, IR_STAGNATION, IR_ITERATION_LIMIT,
+ IR_NUMERICAL_FAILURE) = range(7)
+
 OK, ERR_ARGUMENT, ERR_CUDA, ERR_WORKSPACE, ERR_TIMEOUT, ERR_NOT_BUILT, ERR_UNSUPPORTED = 0, -1, -2, -3, -4, -5, -6
 
 
@@ -98,6 +101,8 @@ SIGNATURES = {
                                              ctypes.POINTER(Report), VP]),
     "spai_adjoint": (ctypes.c_int, [VP, ctypes.c_int64, F64P, F64P, F64P, F64P, ctypes.POINTER(Options),
                                     ctypes.POINTER(Report)]),
+    "spai_adjoint_device": (ctypes.c_int, [VP, ctypes.c_int64, VP, VP, VP, VP, ctypes.POINTER(Options),
+                                           ctypes.POINTER(Report)]),
     "spai_profile": (ctypes.c_int, [VP, ctypes.c_int32]),
     "spai_profile_read": (ctypes.c_int, [VP, ctypes.c_int32, F64P, I64P, F64P]),
     "spai_backward_error_noalloc": (ctypes.c_int, [VP, VP, VP, VP, VP]),
@@ -271,6 +276,13 @@ class Handle:
         _check(lib().spai_adjoint(self._h, nrhs, _p(x, F64P), _p(dldx, F64P), _p(dldb, F64P), _p(dlda, F64P),
                                   ctypes.byref(opts), ctypes.byref(rep)))
         return dldb, dlda, rep.as_dict()
+
+    def adjoint_device(self, nrhs, x_ptr, dldx_ptr, dldb_ptr, dlda_ptr, opts):
+        """Adjoint with device pointers (column-major n x nrhs vectors, nnz gradient values)."""
+        rep = Report()
+        _check(lib().spai_adjoint_device(self._h, nrhs, x_ptr, dldx_ptr, dldb_ptr, dlda_ptr,
+                                         ctypes.byref(opts), ctypes.byref(rep)))
+        return rep.as_dict()
 
 
 def ir_solve(system, b, opts, reference=None, stream=None):

@@ -21,9 +21,10 @@ UNITS = {
     "spai_build.o": ("spai_build.cu", ["--fmad=false"]),
     "api.o": ("api.cu", []),
     "noalloc.o": ("noalloc.cu", []),
+    "batched.o": ("batched.cu", []),
 }
 HEADERS = ["common.cuh", "exact_math.cuh", "spai_internal.hpp", "krylov.cuh", "krylov_kernels.cuh",
-           "mm_io.hpp"]
+           "cgs_tiles.cuh", "adjoint.cuh", "mm_io.hpp"]
 CLIS = {"gpu_fp64_ir": "-DSOLVER_F64", "gpu_fp32_ir": "-DSOLVER_F32", "gpu_mixed_ir": "-DSOLVER_MIXED"}
 
 LIB = os.path.join(OUT, "libspai_ir.so")

@@ -161,6 +161,18 @@ def anisotropic_diffusion(N=256, seed=0, sigma=1.0, corr_len=8.0, anisotropy=10.
     return (n,) + _canonical(n, np.concatenate(R), np.concatenate(C), np.concatenate(V))
 
 
+def differentiation_problem(N=256, nrhs=64, seed=0, perturbation=0.1):
+    """The differentiation workload: anisotropic diffusion on an N x N grid (log-normal coefficient,
+    sigma 1, correlation length 8 cells, anisotropy 10), nrhs N(0,1) right-hand sides (n x nrhs)
+    and the system whose solutions are the targets x* (coefficient field multiplied by a second
+    seeded log-normal field of log-standard-deviation `perturbation`)."""
+    field = _correlated_field(N, seed)
+    system = anisotropic_diffusion(N, field=field)
+    star = anisotropic_diffusion(N, field=field * _correlated_field(N, seed + 1, sigma=perturbation))
+    B = np.random.default_rng(seed + 2).standard_normal((N * N, nrhs))
+    return system, np.asfortranarray(B), star
+
+
 def equal_rhs(n):
     """Equal components with unit 2-norm, the CLI right-hand side (src/solver_main.cpp:94)."""
     return np.full(n, 1.0 / np.sqrt(n))
