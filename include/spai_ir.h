@@ -234,6 +234,12 @@ int spai_profile_read(spai_handle *h, int32_t cls, double *ms, int64_t *launches
 int spai_backward_error_noalloc(spai_handle *h, const double *d_b, const double *d_x,
                                 double *d_out, void *stream);
 
+/* The device's correctly rounded hypot on host arrays (precision 0: binary64, otherwise binary32
+ * on the operands rounded to binary32, widened on return): the function every SPAI column norm
+ * chain calls, exposed so that it can be checked against an independent implementation.
+ * Returns SPAI_OK or an error code. No reference counterpart. */
+int spai_hypot_device(int32_t precision, int64_t count, const double *a, const double *b, double *out);
+
 /* Host builds of the device hypot used by the SPAI fits (parity tests). */
 double spai_hypot(double a, double b);
 float spai_hypotf(float a, float b);

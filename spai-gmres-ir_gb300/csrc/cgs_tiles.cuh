@@ -15,10 +15,22 @@
 // The last block of the finishing pass forms the Hessenberg column (h1 [+ h2], ||w'|| or ||w''||),
 // applies the Givens rotations and sets the acceptance flags, exactly as the single-pass
 // version did. Reductions are deterministic (fixed tile assignment, fixed trees).
+//
+// Streaming: while k + 1 segments fit in a pipeline stage, each block streams its tiles through
+// two shared-memory stages filled by asynchronous 16-byte copies (cp.async, one commit group per
+// stage): a tile's k + 1 segments are contiguous, several tiles share a stage when k is small,
+// and the next stage loads while the current one is consumed. Every warp owns
+// the segments j = warp (mod 8) of every tile: its dots are reduced across lanes into
+// accumulators it alone updates, the update combines the warps' partial sums in a fixed order,
+// and pass 2 takes its second dot product from the resident stage (no re-read). The source
+// vector's segment travels in the same stage.
+// Larger k falls back to chunked cp.async staging.
 #pragma once
 #include "common.cuh"
 #include "exact_math.cuh"
 #include "krylov.cuh"
+
+#include <algorithm>
 
 namespace spai {
 
@@ -78,7 +90,80 @@ template <class T> struct CgsArgs {
     Ctl *ctl;
     CgsScratch scr;
     int always_reorth;
+    int stage_segs;     // segments per pipeline stage (0: always chunked staging)
 };
+
+constexpr int kCgsStages = 2;
+constexpr int kCgsWarps = kCgsThreads / 32;
+
+// Dynamic shared memory of a pass: accumulators and coefficients first, then the staging region
+// (chunk buffer of the chunked path, or the pipeline stages of the streamed one).
+template <class T> __host__ __device__ inline size_t cgs_region_offset(int cap) {
+    return (2 * static_cast<size_t>(cap + 2) * sizeof(T) + 127) & ~static_cast<size_t>(127);
+}
+// Largest stage (in 512-byte segments) that fits beside the accumulators; a tile at step k needs
+// k + 2 segments (basis and source), so cap + 1 covers every step.
+template <class T> inline int cgs_stage_segs(int cap, size_t dyn_budget) {
+    const size_t off = cgs_region_offset<T>(cap);
+    if (off >= dyn_budget)
+        return 0;
+    const size_t segs = (dyn_budget - off) / (static_cast<size_t>(kCgsStages) * 512);
+    return static_cast<int>(std::min<size_t>(segs, static_cast<size_t>(cap) + 1));
+}
+template <class T> inline size_t cgs_dyn_smem(int cap, int stage_segs) {
+    constexpr int R = 512 / sizeof(T);
+    const size_t chunked = (static_cast<size_t>(kCgsJB) * R + R) * sizeof(T);
+    const size_t streamed = static_cast<size_t>(kCgsStages) * stage_segs * 512;
+    return cgs_region_offset<T>(cap) + std::max(chunked, streamed);
+}
+
+// 16-byte vector of T per lane: a warp covers one 512-byte segment.
+template <class T> struct Vec16;
+template <> struct Vec16<float> {
+    using V = float4;
+    static constexpr int E = 4;
+    __device__ __forceinline__ static float dot(V a, V b) {
+        return a.x * b.x + a.y * b.y + a.z * b.z + a.w * b.w;
+    }
+    __device__ __forceinline__ static V axpy(float c, V x, V y) { // y + c x
+        return make_float4(y.x + c * x.x, y.y + c * x.y, y.z + c * x.z, y.w + c * x.w);
+    }
+    __device__ __forceinline__ static V add(V a, V b) {
+        return make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w);
+    }
+    __device__ __forceinline__ static V sub(V a, V b) {
+        return make_float4(a.x - b.x, a.y - b.y, a.z - b.z, a.w - b.w);
+    }
+    __device__ __forceinline__ static V zero() {
+        return make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    __device__ __forceinline__ static float get(V a, int i) {
+        return i == 0 ? a.x : (i == 1 ? a.y : (i == 2 ? a.z : a.w));
+    }
+};
+template <> struct Vec16<double> {
+    using V = double2;
+    static constexpr int E = 2;
+    __device__ __forceinline__ static double dot(V a, V b) {
+        return a.x * b.x + a.y * b.y;
+    }
+    __device__ __forceinline__ static V axpy(double c, V x, V y) {
+        return make_double2(y.x + c * x.x, y.y + c * x.y);
+    }
+    __device__ __forceinline__ static V add(V a, V b) {
+        return make_double2(a.x + b.x, a.y + b.y);
+    }
+    __device__ __forceinline__ static V sub(V a, V b) {
+        return make_double2(a.x - b.x, a.y - b.y);
+    }
+    __device__ __forceinline__ static V zero() {
+        return make_double2(0.0, 0.0);
+    }
+    __device__ __forceinline__ static double get(V a, int i) {
+        return i == 0 ? a.x : a.y;
+    }
+};
+
 
 // cp.async 16-byte copies global -> shared (no spin-wait; completion via wait_group).
 __device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
@@ -185,10 +270,11 @@ __global__ void __launch_bounds__(kCgsThreads) cgs_pass_kernel(CgsArgs<T> a) {
     if (MODE == 3 && !ctl->reorth)
         return;
     extern __shared__ __align__(16) unsigned char dyn[];
-    T *buf = reinterpret_cast<T *>(dyn);            // [kCgsJB * R]
-    T *wt = buf + kCgsJB * R;                        // [R]
-    T *acc = wt + R;                                 // [cap + 2] dot accumulators
-    T *cf = acc + (ctl->cap + 2);                    // [cap + 2] update coefficients h_j s_j
+    T *acc = reinterpret_cast<T *>(dyn);                           // [cap + 2] dot accumulators
+    T *cf = acc + (ctl->cap + 2);                                   // [cap + 2] update coefficients h_j s_j
+    T *region = reinterpret_cast<T *>(dyn + cgs_region_offset<T>(ctl->cap)); // staging (128-byte aligned)
+    T *buf = region;                                                // chunked path: [kCgsJB * R]
+    T *wt = buf + kCgsJB * R;                                       // chunked path: [R]
     constexpr int NP = kCgsThreads / R; // threads per row in the update
     __shared__ T red[kCgsThreads / 32];
     __shared__ T part_sum[NP][R];
@@ -206,7 +292,113 @@ __global__ void __launch_bounds__(kCgsThreads) cgs_pass_kernel(CgsArgs<T> a) {
     int te = INT_MIN;
     T ts = 0;
     bool bad = false;
-    for (int t = blockIdx.x; t < a.V.ntiles; t += gridDim.x) {
+    auto ssq_add = [&](T v) {
+        bad |= !isfinite(v);
+        if (v != T(0) && isfinite(v)) {
+            const int ev = ilogb(v);
+            if (ev > te) {
+                if (te != INT_MIN)
+                    ts = ldexp(ts, 2 * (te - ev));
+                te = ev;
+            }
+            const T sv = ldexp(v, -te);
+            ts += sv * sv;
+        }
+    };
+    // A tile occupies kk + 1 segments of a stage: W_0..W_k, then the source vector's segment (w
+    // for passes 1 and 2, W_{k+1} for pass 3), so no tile waits on a dependent global load.
+    const int tseg = kk + 1;
+    const bool streamed = tseg <= a.stage_segs;
+    if (streamed) {
+        // ---- Streamed path: whole tiles through kCgsStages double-buffered stages. ----
+        using VT = Vec16<T>;
+        using V16 = typename VT::V;
+        constexpr int E = VT::E;
+        __shared__ __align__(16) V16 wpart[2][kCgsWarps][32];
+        T *stage0 = region;
+        const size_t stage_elems = static_cast<size_t>(a.stage_segs) * R;
+        const int tt_per = max(1, a.stage_segs / tseg); // tiles per stage
+        const int my_tiles = a.V.ntiles > static_cast<int>(blockIdx.x)
+                                 ? (a.V.ntiles - 1 - static_cast<int>(blockIdx.x)) / static_cast<int>(gridDim.x) + 1
+                                 : 0;
+        const int nitems = (my_tiles + tt_per - 1) / tt_per;
+        const int basis_bytes = (MODE == 3 ? tseg : kk) * R * static_cast<int>(sizeof(T));
+        constexpr int kSegBytes = R * static_cast<int>(sizeof(T));
+        // Every thread issues 16-byte asynchronous copies for an item's tiles; one commit group per
+        // item (empty past the end), so "all but the newest group complete" means "item ready".
+        auto issue = [&](int item) {
+            if (item < nitems) {
+                const int st = item % kCgsStages;
+                const int q0 = item * tt_per;
+                const int q1 = min(my_tiles, q0 + tt_per);
+                for (int q = q0; q < q1; ++q) {
+                    const int t = static_cast<int>(blockIdx.x) + q * static_cast<int>(gridDim.x);
+                    char *dst = reinterpret_cast<char *>(stage0 + st * stage_elems + static_cast<size_t>(q - q0) * tseg * R);
+                    const char *src = reinterpret_cast<const char *>(a.V.seg(t, 0));
+                    for (int o = threadIdx.x * 16; o < basis_bytes; o += kCgsThreads * 16)
+                        cp_async16(dst + o, src + o);
+                    if (MODE != 3) {
+                        const char *ws = reinterpret_cast<const char *>(a.w + static_cast<long long>(t) * R);
+                        for (int o = threadIdx.x * 16; o < kSegBytes; o += kCgsThreads * 16)
+                            cp_async16(dst + kk * kSegBytes + o, ws + o);
+                    }
+                }
+            }
+            asm volatile("cp.async.commit_group;\n" ::: "memory");
+        };
+        __syncthreads(); // coefficients visible
+        for (int i = 0; i < kCgsStages; ++i)
+            issue(i);
+        int flip = 0;
+        for (int item = 0; item < nitems; ++item) {
+            const int st = item % kCgsStages;
+            asm volatile("cp.async.wait_group %0;\n" ::"n"(kCgsStages - 1) : "memory");
+            __syncthreads();
+            const T *sbase = stage0 + st * stage_elems;
+            const int q0 = item * tt_per;
+            const int q1 = min(my_tiles, q0 + tt_per);
+            for (int q = q0; q < q1; ++q) {
+                const int t = static_cast<int>(blockIdx.x) + q * static_cast<int>(gridDim.x);
+                const T *tile = sbase + static_cast<size_t>(q - q0) * tseg * R;
+                V16 cur = *reinterpret_cast<const V16 *>(tile + kk * R + lane * E);
+                // Warp w owns the segments j = w (mod 8): balanced at every k, and each dot
+                // accumulator has one owner (deterministic, no atomics).
+                if (MODE >= 2) {
+                    V16 part = VT::zero();
+#pragma unroll 4
+                    for (int j = warp; j < kk; j += kCgsWarps)
+                        part = VT::axpy(cf[j], *reinterpret_cast<const V16 *>(tile + j * R + lane * E), part);
+                    wpart[flip][warp][lane] = part;
+                    __syncthreads();
+                    V16 tot = wpart[flip][0][lane];
+#pragma unroll
+                    for (int q2 = 1; q2 < kCgsWarps; ++q2)
+                        tot = VT::add(tot, wpart[flip][q2][lane]);
+                    cur = VT::sub(cur, tot); // pad rows: every operand is zero there
+                    if (warp == 0)
+                        *reinterpret_cast<V16 *>(a.V.seg(t, kk) + lane * E) = cur; // W_{k+1}
+                    flip ^= 1;
+                }
+                if (warp == 0)
+                    for (int e = 0; e < E; ++e)
+                        ssq_add(VT::get(cur, e));
+                if (MODE <= 2) {
+#pragma unroll 2
+                    for (int j = warp; j < kk; j += kCgsWarps) {
+                        T d = VT::dot(*reinterpret_cast<const V16 *>(tile + j * R + lane * E), cur);
+                        for (int o = 16; o > 0; o >>= 1)
+                            d += __shfl_xor_sync(0xffffffffu, d, o);
+                        if (lane == 0)
+                            acc[j] += d;
+                    }
+                }
+            }
+            __syncthreads(); // the stage is free
+            issue(item + kCgsStages);
+        }
+        asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+    }
+    for (int t = blockIdx.x; !streamed && t < a.V.ntiles; t += gridDim.x) {
         const int row0 = t * R;
         const int rows = min(R, a.n - row0);
         __syncthreads();
@@ -267,20 +459,8 @@ __global__ void __launch_bounds__(kCgsThreads) cgs_pass_kernel(CgsArgs<T> a) {
                 __syncthreads();
             }
         }
-        if (threadIdx.x < R) {
-            const T v = wt[threadIdx.x];
-            bad |= !isfinite(v);
-            if (v != T(0) && isfinite(v)) {
-                const int ev = ilogb(v);
-                if (ev > te) {
-                    if (te != INT_MIN)
-                        ts = ldexp(ts, 2 * (te - ev));
-                    te = ev;
-                }
-                const T sv = ldexp(v, -te);
-                ts += sv * sv;
-            }
-        }
+        if (threadIdx.x < R)
+            ssq_add(wt[threadIdx.x]);
     }
     // Block combine of the per-thread (te, ts) pairs: common exponent, then a fixed-order sum.
     int be = te;

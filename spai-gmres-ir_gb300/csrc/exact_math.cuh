@@ -153,6 +153,73 @@ SPAI_HD int em_midpoint_sign(T c, T half, int sgn, T xx, T xxe, T yy, T yye) {
     return em_exact_sign(t, 8);
 }
 
+#ifdef __CUDA_ARCH__
+// Device fast path for normal operands: exponents and power-of-two scales from the bit fields,
+// and a division-free acceptance test. With x >= y scaled to xs in [1, 2), the candidate
+// c = fl(sqrt(fl(xs^2 + ys^2))) is the correctly rounded value iff |t - c| < h, t the exact
+// value and h the distance from c to the nearer rounding midpoint (ulp(c)/2, or ulp(c)/4 below
+// a power of two). Since |t - c| = |R| / (t + c) with R = xs^2 + ys^2 - c^2 (computed to within
+// a few units of 2^-48 c^2 by error-free transformations), |R| < 2 c h (1 - 2^-16) is sufficient.
+// Returns false (nothing decided) when an operand is subnormal or too large for the scaling, or
+// when the test does not accept; the caller then takes the general path, so the result is the
+// same correctly rounded value either way.
+__device__ __forceinline__ bool cr_hypot_fast(float x, float y, float &out) {
+    const unsigned bx = __float_as_uint(x), by = __float_as_uint(y);
+    const int fx = static_cast<int>(bx >> 23), fy = static_cast<int>(by >> 23);
+    if (fy == 0 || fx > 253)
+        return false;
+    if (fx - fy > 14) { // y/x < 2^-14: the exact value rounds to x
+        out = x;
+        return true;
+    }
+    const float scale = __uint_as_float(static_cast<unsigned>(254 - fx) << 23); // 2^(127 - fx)
+    const float xs = x * scale, ys = y * scale;
+    float xx, xxe, yy, yye, p, pe, sh, sl;
+    em_two_prod(xs, xs, xx, xxe);
+    em_two_prod(ys, ys, yy, yye);
+    const float c = __fsqrt_rn(__fadd_rn(xx, yy));
+    em_two_prod(c, c, p, pe);
+    em_two_sum(xx, yy, sh, sl);
+    const float r = __fadd_rn(__fsub_rn(sh, p), __fadd_rn(__fsub_rn(sl, pe), __fadd_rn(xxe, yye)));
+    const unsigned bc = __float_as_uint(c);
+    const unsigned hb = (bc & 0x7f800000u) - (24u << 23) - ((bc & 0x007fffffu) == 0 ? (1u << 23) : 0u);
+    const float thr = __fmul_rn(__fmul_rn(__fadd_rn(c, c), __uint_as_float(hb)), 0.9999847412109375f);
+    if (!(fabsf(r) < thr))
+        return false;
+    out = __fmul_rn(c, __uint_as_float(static_cast<unsigned>(fx) << 23)); // c * 2^(fx - 127), exact
+    return true;
+}
+__device__ __forceinline__ bool cr_hypot_fast(double x, double y, double &out) {
+    const unsigned long long bx = static_cast<unsigned long long>(__double_as_longlong(x));
+    const unsigned long long by = static_cast<unsigned long long>(__double_as_longlong(y));
+    const int fx = static_cast<int>(bx >> 52), fy = static_cast<int>(by >> 52);
+    if (fy == 0 || fx > 2045)
+        return false;
+    if (fx - fy > 30) {
+        out = x;
+        return true;
+    }
+    const double scale = __longlong_as_double(static_cast<long long>(2046 - fx) << 52); // 2^(1023 - fx)
+    const double xs = x * scale, ys = y * scale;
+    double xx, xxe, yy, yye, p, pe, sh, sl;
+    em_two_prod(xs, xs, xx, xxe);
+    em_two_prod(ys, ys, yy, yye);
+    const double c = __dsqrt_rn(__dadd_rn(xx, yy));
+    em_two_prod(c, c, p, pe);
+    em_two_sum(xx, yy, sh, sl);
+    const double r = __dadd_rn(__dsub_rn(sh, p), __dadd_rn(__dsub_rn(sl, pe), __dadd_rn(xxe, yye)));
+    const unsigned long long bc = static_cast<unsigned long long>(__double_as_longlong(c));
+    const unsigned long long hb = (bc & 0x7ff0000000000000ull) - (53ull << 52) -
+                                  ((bc & 0x000fffffffffffffull) == 0 ? (1ull << 52) : 0ull);
+    const double thr = __dmul_rn(__dmul_rn(__dadd_rn(c, c), __longlong_as_double(static_cast<long long>(hb))),
+                                 0.99999999999909050530);
+    if (!(fabs(r) < thr))
+        return false;
+    out = __dmul_rn(c, __longlong_as_double(static_cast<long long>(fx) << 52)); // c * 2^(fx - 1023)
+    return true;
+}
+#endif
+
 // Correctly rounded (to nearest, ties to even) hypot in T = double or float.
 template <class T> SPAI_HD T cr_hypot(T a, T b) {
     T x = std::fabs(a), y = std::fabs(b);
@@ -167,6 +234,13 @@ template <class T> SPAI_HD T cr_hypot(T a, T b) {
     }
     if (y == 0)
         return x;
+#ifdef __CUDA_ARCH__
+    {
+        T fast;
+        if (cr_hypot_fast(x, y, fast))
+            return fast;
+    }
+#endif
     const int ex = em_ilogb(x), ey = em_ilogb(y);
     // y/x below 2^-(p/2+2) with p the significand width: the exact value rounds to x.
     if (ex - ey > (sizeof(T) == 8 ? 30 : 14))

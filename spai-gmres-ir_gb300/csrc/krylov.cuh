@@ -43,7 +43,7 @@ struct Ctl {
     double be_tol;
     double den, beta, est, hnext, rel, orig;
     int outer_cap;
-    int counters[16]; // last-block tickets
+    int counters[16];   // spare
 };
 
 struct GmresBuffers; // defined in krylov.cu

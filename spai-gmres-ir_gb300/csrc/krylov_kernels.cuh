@@ -21,6 +21,7 @@
 #pragma once
 #include "krylov.cuh"
 #include "cgs_tiles.cuh"
+#include "sell.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -642,6 +643,34 @@ void launch_spmv(const DeviceCsr<TA> &m, VecRef<TX> x, VecRef<TY> y, const int *
     SPAI_LAUNCH("spmv_kernel");
 }
 
+// Sliced-ELLPACK SpMVs (one warp per 32-row slice) for the Krylov operators.
+template <class T>
+__global__ void __launch_bounds__(kBlock) sell_spmv_kernel(DeviceSell<T> m, VecRef<T> x, VecRef<T> y,
+                                                           const int *gate) {
+    if (gate && !*gate)
+        return;
+    const T *xv = x.get();
+    sell_rows(m, [&](int c) { return xv[c]; }, T(1), y.get());
+}
+// t = s_k A W_k with W_k gathered from the tile-major basis.
+template <class T>
+__global__ void __launch_bounds__(kBlock) sell_spmv_basis_kernel(DeviceSell<T> m, Basis<T> V, T *y,
+                                                                 const Ctl *ctl) {
+    constexpr int R = TileGeom<T>::R;
+    if (!ctl->active)
+        return;
+    const int k = ctl->k;
+    const T *base = V.base + static_cast<long long>(k) * R;
+    const long long tstride = static_cast<long long>(V.cap1) * R;
+    sell_rows(m, [&](int c) { return base[(c / R) * tstride + (c % R)]; }, V.scale[k], y);
+}
+template <class T>
+void launch_sell(const DeviceSell<T> &m, VecRef<T> x, VecRef<T> y, const int *gate, int sms, cudaStream_t st) {
+    const unsigned blocks = grid_for(static_cast<long long>(m.nslices) * 32, kBlock, sms * 8);
+    sell_spmv_kernel<T><<<blocks, kBlock, 0, st>>>(m, x, y, gate);
+    SPAI_LAUNCH("sell_spmv_kernel");
+}
+
 // Optional per-kernel-class timing: CUDA events recorded on the solve stream around each
 // launch of the Arnoldi kernels. Launch records of speculative steps past the end of a GMRES
 // solve are discarded using the solve's iteration count.
@@ -707,6 +736,7 @@ template <class T, class TO> struct IrEngine {
     const DeviceCsr<TO> *a_outer = nullptr;
     const DeviceCsr<T> *a_inner = nullptr;
     const DeviceCsr<T> *p = nullptr;
+    DeviceSell<T> sa, sp; // sliced companions of the inner matrix and of P
     Ctl *ctl = nullptr;
     T *V = nullptr, *sc = nullptr, *w = nullptr, *t = nullptr, *rhs = nullptr, *pb = nullptr, *cand = nullptr,
       *ax = nullptr, *pax = nullptr, *H = nullptr, *cs = nullptr, *sn = nullptr, *g = nullptr,
@@ -716,6 +746,8 @@ template <class T, class TO> struct IrEngine {
     DiagPart *dpart = nullptr;
     int *counters = nullptr;
     int nblk_vec = 0, nblk_dots = 0, ntiles = 0;
+    int stage_segs = 0;   // Gram-Schmidt pipeline stage size (segments)
+    size_t cgs_dyn = 0;   // dynamic shared memory of a pass
     void *cgs_dots = nullptr, *cgs_norms = nullptr;
     bool always_reorth = false;
     int *pinned_host = nullptr; // host flag for profile-mode reads
@@ -855,24 +887,35 @@ template <class T, class TO> struct IrEngine {
         n = ai.n;
         cap = cap_;
         sms = sms_;
-        ld = (static_cast<long long>(n) + 31) & ~31LL;
+        // Vectors are padded to whole basis tiles: the streamed Gram-Schmidt passes read the
+        // source vector tile by tile (pad rows of w are zero and never written).
+        ld = ((static_cast<long long>(n) + TileGeom<T>::R - 1) / TileGeom<T>::R) * TileGeom<T>::R;
         hld = cap + 2;
         nblk_vec = static_cast<int>(grid_for(n, kBlock, sms * 8));
         constexpr int R = TileGeom<T>::R;
         ntiles = (n + R - 1) / R;
-        nblk_dots = std::min(ntiles, sms * 2);
+        // One block per SM: the pipeline stages take most of the shared memory (the static
+        // arrays of the pass use about 10 KiB of the 227 KiB).
+        stage_segs = cgs_stage_segs<T>(cap, 216 * 1024);
+        cgs_dyn = cgs_dyn_smem<T>(cap, stage_segs);
+        nblk_dots = std::min(ntiles, sms);
         ctl = arena.alloc<Ctl>(1);
+        cudaStream_t setup_st = nullptr;
+        sa = build_sell(arena, ai, sms, setup_st);
+        sp = build_sell(arena, pp, sms, setup_st);
+        SPAI_CUDA(cudaStreamSynchronize(setup_st));
         const size_t vcount = static_cast<size_t>(ntiles) * (cap + 1) * R;
         V = arena.alloc<T>(vcount);
         SPAI_CUDA(cudaMemset(V, 0, vcount * sizeof(T))); // pad rows of the last tile stay zero
         sc = arena.alloc<T>(cap + 2);
         cgs_dots = arena.alloc<T>(static_cast<size_t>(nblk_dots) * (cap + 2));
         cgs_norms = arena.alloc<Ssq<T>>(nblk_dots);
-        const int smem = static_cast<int>(cgs_smem_for(cap));
+        const int smem = static_cast<int>(cgs_dyn);
         SPAI_CUDA(cudaFuncSetAttribute(cgs_pass_kernel<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
         SPAI_CUDA(cudaFuncSetAttribute(cgs_pass_kernel<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
         SPAI_CUDA(cudaFuncSetAttribute(cgs_pass_kernel<T, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
         w = arena.alloc<T>(ld);
+        SPAI_CUDA(cudaMemset(w, 0, sizeof(T) * ld));
         t = arena.alloc<T>(ld);
         rhs = arena.alloc<T>(ld);
         pb = arena.alloc<T>(ld);
@@ -906,13 +949,11 @@ template <class T, class TO> struct IrEngine {
     }
     CgsArgs<T> cgs_args() const {
         return CgsArgs<T>{n, basis(), w, h1, h2, H, cs, sn, g, sc, hld, ctl,
-                          CgsScratch{cgs_dots, cgs_norms, counters + kSlotDots}, always_reorth ? 1 : 0};
-    }
-    static size_t cgs_smem_for(int cap_) {
-        return sizeof(T) * (static_cast<size_t>(kCgsJB) * TileGeom<T>::R + TileGeom<T>::R + 2 * (cap_ + 2));
+                          CgsScratch{cgs_dots, cgs_norms, counters + kSlotDots}, always_reorth ? 1 : 0,
+                          stage_segs};
     }
     size_t cgs_smem() const {
-        return cgs_smem_for(cap);
+        return cgs_dyn;
     }
 
     void norm(cudaStream_t st, VecRef<T> a, const T *bsub, T *out, int slot, const int *gate) {
@@ -951,26 +992,15 @@ template <class T, class TO> struct IrEngine {
         // w = P·(A v) (left) or w = A·(P v) (right): the first matrix gathers the basis vector.
         const DeviceCsr<T> &m1 = right ? *p : *a_inner;
         const DeviceCsr<T> &m2 = right ? *a_inner : *p;
+        const DeviceSell<T> &s1 = right ? sp : sa;
+        const DeviceSell<T> &s2 = right ? sa : sp;
         timed(st, kClsSpmvA, spmv_bytes(m1), [&] {
-            const int G = pick_group(m1);
-            const unsigned blocks = grid_for(static_cast<long long>(n) * G, 256, sms * 16);
-            const Basis<T> vb = basis();
-#define SPAI_SPMV_BASIS(g)                                                                         \
-    case g:                                                                                        \
-        spmv_basis_kernel<T, g><<<blocks, 256, 0, st>>>(n, m1.rp, m1.ci, m1.val, vb, t, ctl);      \
-        break;
-            switch (G) {
-                SPAI_SPMV_BASIS(2)
-                SPAI_SPMV_BASIS(4)
-                SPAI_SPMV_BASIS(8)
-                SPAI_SPMV_BASIS(16)
-                SPAI_SPMV_BASIS(32)
-            }
-#undef SPAI_SPMV_BASIS
-            SPAI_LAUNCH("spmv_basis_kernel");
+            const unsigned blocks = grid_for(static_cast<long long>(s1.nslices) * 32, kBlock, sms * 8);
+            sell_spmv_basis_kernel<T><<<blocks, kBlock, 0, st>>>(s1, basis(), t, ctl);
+            SPAI_LAUNCH("sell_spmv_basis_kernel");
         });
         timed(st, kClsSpmvP, spmv_bytes(m2), [&] {
-            launch_spmv<T, T, T>(m2, fixed(t), fixed(w), &ctl->active, sms, st);
+            launch_sell<T>(s2, fixed(t), fixed(w), &ctl->active, sms, st);
         });
         const size_t smem = cgs_smem();
         const CgsArgs<T> args = cgs_args();
@@ -1013,17 +1043,17 @@ template <class T, class TO> struct IrEngine {
             // residual unpreconditioned, so it is also the decision's numerator).
             form_candidate_tiles_kernel<T><<<nblk_vec, kBlock, 0, st>>>(n, basis(), y, pax, ctl);
             SPAI_LAUNCH("form_candidate_tiles_kernel");
-            launch_spmv<T, T, T>(*p, fixed(pax), fixed(cand), g2, sms, st);
-            launch_spmv<T, T, T>(*a_inner, fixed(cand), fixed(ax), g2, sms, st);
+            launch_sell<T>(sp, fixed(pax), fixed(cand), g2, sms, st);
+            launch_sell<T>(sa, fixed(cand), fixed(ax), g2, sms, st);
             norm(st, fixed(rhs), ax, scal + 0, kSlotNormA, g2);
             launches += 3;
             return;
         }
         form_candidate_tiles_kernel<T><<<nblk_vec, kBlock, 0, st>>>(n, basis(), y, cand, ctl);
         SPAI_LAUNCH("form_candidate_tiles_kernel");
-        launch_spmv<T, T, T>(*a_inner, fixed(cand), fixed(ax), g2, sms, st);
+        launch_sell<T>(sa, fixed(cand), fixed(ax), g2, sms, st);
         norm(st, fixed(rhs), ax, scal + 0, kSlotNormA, g2);
-        launch_spmv<T, T, T>(*p, fixed(ax), fixed(pax), g2, sms, st);
+        launch_sell<T>(sp, fixed(ax), fixed(pax), g2, sms, st);
         norm(st, fixed(pb), pax, scal + 1, kSlotNormB, g2);
         launches += 4;
     }
@@ -1035,7 +1065,7 @@ template <class T, class TO> struct IrEngine {
         gmres_start_kernel<T><<<1, 32, 0, st>>>(ctl, scal + 2, accept_every ? 1 : 0);
         SPAI_LAUNCH("gmres_start_kernel");
         if (!right) {
-            launch_spmv<T, T, T>(*p, fixed(rhs), fixed(pb), &ctl->active, sms, st);
+            launch_sell<T>(sp, fixed(rhs), fixed(pb), &ctl->active, sms, st);
             ++launches;
         }
         norm(st, fixed(const_cast<T *>(pbv())), nullptr, scal + 3, kSlotNormB, &ctl->active);

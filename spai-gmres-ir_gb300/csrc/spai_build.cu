@@ -1198,6 +1198,39 @@ template void score_kat<float>(float, float, float, double *);
 
 } // namespace spai
 
+namespace spai {
+__global__ void hypot_eval_kernel(int precision, long long count, const double *a, const double *b, double *out) {
+    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < count;
+         i += static_cast<long long>(gridDim.x) * blockDim.x)
+        out[i] = precision == 0 ? cr_hypot<double>(a[i], b[i])
+                                : static_cast<double>(cr_hypot<float>(static_cast<float>(a[i]), static_cast<float>(b[i])));
+}
+} // namespace spai
+
+// The device hypot on host arrays (precision 0: binary64; otherwise binary32 on the operands
+// rounded to binary32, returned widened). Check hook for the SPAI norm chains.
+extern "C" int spai_hypot_device(int32_t precision, int64_t count, const double *a, const double *b, double *out) {
+    if (count < 0 || (count > 0 && (!a || !b || !out)))
+        return spai_api_fail(-1, "spai_hypot_device: bad arguments");
+    if (count == 0)
+        return 0;
+    try {
+        double *d = nullptr;
+        const size_t bytes = sizeof(double) * static_cast<size_t>(count);
+        SPAI_CUDA(cudaMalloc(&d, 3 * bytes));
+        SPAI_CUDA(cudaMemcpy(d, a, bytes, cudaMemcpyHostToDevice));
+        SPAI_CUDA(cudaMemcpy(d + count, b, bytes, cudaMemcpyHostToDevice));
+        spai::hypot_eval_kernel<<<spai::grid_for(count, 256, 152 * 8), 256>>>(precision, count, d, d + count, d + 2 * count);
+        const cudaError_t e = cudaGetLastError();
+        SPAI_CUDA(cudaMemcpy(out, d + 2 * count, bytes, cudaMemcpyDeviceToHost));
+        cudaFree(d);
+        SPAI_CUDA(e);
+    } catch (const std::exception &e) {
+        return spai_api_fail(-2, e.what());
+    }
+    return 0;
+}
+
 extern "C" double spai_hypot(double a, double b) {
     return spai::cr_hypot<double>(a, b);
 }

@@ -106,6 +106,7 @@ SIGNATURES = {
     "spai_profile": (ctypes.c_int, [VP, ctypes.c_int32]),
     "spai_profile_read": (ctypes.c_int, [VP, ctypes.c_int32, F64P, I64P, F64P]),
     "spai_backward_error_noalloc": (ctypes.c_int, [VP, VP, VP, VP, VP]),
+    "spai_hypot_device": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int64, F64P, F64P, F64P]),
     "spai_hypot": (ctypes.c_double, [ctypes.c_double, ctypes.c_double]),
     "spai_hypotf": (ctypes.c_float, [ctypes.c_float, ctypes.c_float]),
 }
@@ -314,6 +315,15 @@ def score(rsq, dot, den, precision="f64"):
     out = np.zeros(3)
     _check(lib().spai_score(PRECISION[precision], rsq, dot, den, _p(out, F64P)))
     return int(out[0]), float(out[1]), bool(out[2])
+
+
+def hypot_device(a, b, precision="f64"):
+    """The device hypot on arrays (binary32 for precision "f32": operands rounded, result widened)."""
+    a = np.ascontiguousarray(a, np.float64)
+    b = np.ascontiguousarray(b, np.float64)
+    out = np.zeros(len(a))
+    _check(lib().spai_hypot_device(0 if precision == "f64" else 1, len(a), _p(a, F64P), _p(b, F64P), _p(out, F64P)))
+    return out
 
 
 def hypot(a, b):

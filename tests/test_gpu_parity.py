@@ -274,3 +274,53 @@ def test_cli_c1_matches_oracle(built, tmp_path):
     xo, ro = O.ir(system, M.equal_rhs(system[0]), alpha=(4096 + 7) // 8)
     assert ro["converged"] and len(x) == 4096
     assert np.max(np.abs(x - xo)) <= 1e-12 * np.max(np.abs(xo)) * 100
+
+
+# ---------------------------------------------------------------------------------------------
+# The device hypot (every SPAI norm chain) is correctly rounded: bit-identical to the oracle's.
+# ---------------------------------------------------------------------------------------------
+def _hypot_cases_f32(rng, count):
+    m = rng.uniform(1, 2, (2, count))
+    e1 = rng.integers(-60, 60, count)
+    gap = rng.integers(0, 20, count)
+    a = np.ldexp(m[0], e1).astype(np.float32)
+    b = np.ldexp(m[1], e1 - gap).astype(np.float32)
+    # Near rounding midpoints: hypot(x, y) within an ulp fraction of c + ulp(c)/2.
+    c = rng.uniform(1, 2, count).astype(np.float32)
+    mid = c.astype(np.float64) + np.spacing(c).astype(np.float64) / 2
+    x = (mid * rng.uniform(0.3, 0.95, count)).astype(np.float32)
+    y = np.sqrt(mid * mid - x.astype(np.float64) ** 2).astype(np.float32)
+    yu = np.nextafter(y, np.float32(np.inf))
+    trip = np.array([3, 4, 5, 8, 15, 17, 20, 21, 29], np.float32)
+    return (np.concatenate([a, x, x, trip[:4]]).astype(np.float64),
+            np.concatenate([b, y, yu, trip[4:8]]).astype(np.float64))
+
+
+def _hypot_cases_f64(rng, count):
+    from decimal import Decimal, getcontext
+
+    getcontext().prec = 60
+    m = rng.uniform(1, 2, (2, count))
+    e1 = rng.integers(-300, 300, count)
+    gap = rng.integers(0, 40, count)
+    a, b = np.ldexp(m[0], e1), np.ldexp(m[1], e1 - gap)
+    near = count // 10
+    c = rng.uniform(1, 2, near)
+    xs, ys = [], []
+    for ci, f in zip(c, rng.uniform(0.3, 0.95, near)):
+        mid = Decimal(float(ci)) + Decimal(float(np.spacing(ci))) / 2
+        x = float(mid * Decimal(float(f)))
+        ys.append(float((mid * mid - Decimal(x) * Decimal(x)).sqrt()))
+        xs.append(x)
+    return np.concatenate([a, xs]), np.concatenate([b, ys])
+
+
+@pytest.mark.parametrize("prec", ["f32", "f64"])
+def test_device_hypot_matches_oracle(built, prec):
+    rng = np.random.default_rng(77)
+    a, b = (_hypot_cases_f32 if prec == "f32" else _hypot_cases_f64)(rng, 200000)
+    got = spai_ir.hypot_device(a, b, prec)
+    ref = O.hypotf if prec == "f32" else O.hypot
+    want = np.array([ref(float(u), float(v)) for u, v in zip(a, b)])
+    bad = np.flatnonzero(got != want)
+    assert bad.size == 0, [(a[i], b[i], got[i], want[i]) for i in bad[:5]]
