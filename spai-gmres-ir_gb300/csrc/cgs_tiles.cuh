@@ -91,30 +91,41 @@ template <class T> struct CgsArgs {
     CgsScratch scr;
     int always_reorth;
     int stage_segs;     // segments per pipeline stage (0: always chunked staging)
+    T *gacc;            // large caps: per-block dot accumulators and coefficients in global memory
+    T *gcf;             //   ([gridDim][cap + 2] each); nullptr: both in shared memory
 };
 
 constexpr int kCgsStages = 2;
 constexpr int kCgsWarps = kCgsThreads / 32;
 
-// Dynamic shared memory of a pass: accumulators and coefficients first, then the staging region
-// (chunk buffer of the chunked path, or the pipeline stages of the streamed one).
-template <class T> __host__ __device__ inline size_t cgs_region_offset(int cap) {
-    return (2 * static_cast<size_t>(cap + 2) * sizeof(T) + 127) & ~static_cast<size_t>(127);
+// Dynamic shared memory of a pass: accumulators, coefficients and per-warp accumulators first,
+// then the staging region (chunk buffer of the chunked path, or the stages of the streamed one).
+// Accumulators and coefficients ([cap + 2] each) live in shared memory up to this size, in
+// per-block global scratch beyond it (very long GMRES caps). Per-warp accumulators hold
+// stage_segs entries each (the streamed path runs only while k + 2 <= stage_segs).
+constexpr size_t kCgsSharedAccMax = 64 * 1024;
+template <class T> __host__ __device__ inline bool cgs_acc_global(int cap) {
+    return 2 * static_cast<size_t>(cap + 2) * sizeof(T) > kCgsSharedAccMax;
+}
+template <class T> __host__ __device__ inline size_t cgs_region_offset(int cap, int stage_segs) {
+    const size_t accs = cgs_acc_global<T>(cap) ? 0 : 2 * static_cast<size_t>(cap + 2);
+    return ((accs + static_cast<size_t>(kCgsWarps) * stage_segs) * sizeof(T) + 127) & ~static_cast<size_t>(127);
 }
 // Largest stage (in 512-byte segments) that fits beside the accumulators; a tile at step k needs
 // k + 2 segments (basis and source), so cap + 1 covers every step.
 template <class T> inline int cgs_stage_segs(int cap, size_t dyn_budget) {
-    const size_t off = cgs_region_offset<T>(cap);
-    if (off >= dyn_budget)
+    const size_t fixed = (cgs_acc_global<T>(cap) ? 0 : 2 * static_cast<size_t>(cap + 2) * sizeof(T)) + 128;
+    if (fixed >= dyn_budget)
         return 0;
-    const size_t segs = (dyn_budget - off) / (static_cast<size_t>(kCgsStages) * 512);
+    const size_t per_seg = static_cast<size_t>(kCgsStages) * 512 + static_cast<size_t>(kCgsWarps) * sizeof(T);
+    const size_t segs = (dyn_budget - fixed) / per_seg;
     return static_cast<int>(std::min<size_t>(segs, static_cast<size_t>(cap) + 1));
 }
 template <class T> inline size_t cgs_dyn_smem(int cap, int stage_segs) {
     constexpr int R = 512 / sizeof(T);
     const size_t chunked = (static_cast<size_t>(kCgsJB) * R + R) * sizeof(T);
     const size_t streamed = static_cast<size_t>(kCgsStages) * stage_segs * 512;
-    return cgs_region_offset<T>(cap) + std::max(chunked, streamed);
+    return cgs_region_offset<T>(cap, stage_segs) + std::max(chunked, streamed);
 }
 
 // 16-byte vector of T per lane: a warp covers one 512-byte segment.
@@ -270,9 +281,14 @@ __global__ void __launch_bounds__(kCgsThreads) cgs_pass_kernel(CgsArgs<T> a) {
     if (MODE == 3 && !ctl->reorth)
         return;
     extern __shared__ __align__(16) unsigned char dyn[];
-    T *acc = reinterpret_cast<T *>(dyn);                           // [cap + 2] dot accumulators
-    T *cf = acc + (ctl->cap + 2);                                   // [cap + 2] update coefficients h_j s_j
-    T *region = reinterpret_cast<T *>(dyn + cgs_region_offset<T>(ctl->cap)); // staging (128-byte aligned)
+    const bool gacc = a.gacc != nullptr;
+    T *acc = gacc ? a.gacc + static_cast<size_t>(blockIdx.x) * (ctl->cap + 2)
+                  : reinterpret_cast<T *>(dyn);                     // [cap + 2] dot accumulators
+    T *cf = gacc ? a.gcf + static_cast<size_t>(blockIdx.x) * (ctl->cap + 2)
+                 : acc + (ctl->cap + 2);                            // [cap + 2] update coefficients h_j s_j
+    T *accw = gacc ? reinterpret_cast<T *>(dyn)
+                   : cf + (ctl->cap + 2);                           // [warps][stage_segs] streamed path
+    T *region = reinterpret_cast<T *>(dyn + cgs_region_offset<T>(ctl->cap, a.stage_segs)); // staging (128-byte aligned)
     T *buf = region;                                                // chunked path: [kCgsJB * R]
     T *wt = buf + kCgsJB * R;                                       // chunked path: [R]
     constexpr int NP = kCgsThreads / R; // threads per row in the update
@@ -314,10 +330,18 @@ __global__ void __launch_bounds__(kCgsThreads) cgs_pass_kernel(CgsArgs<T> a) {
         using VT = Vec16<T>;
         using V16 = typename VT::V;
         constexpr int E = VT::E;
-        __shared__ __align__(16) V16 wpart[2][kCgsWarps][32];
+        __shared__ __align__(16) V16 wpart[kCgsWarps][32];
+        const int cs = a.stage_segs;
+        for (int i = threadIdx.x; i < kCgsWarps * cs; i += blockDim.x)
+            accw[i] = 0;
         T *stage0 = region;
         const size_t stage_elems = static_cast<size_t>(a.stage_segs) * R;
         const int tt_per = max(1, a.stage_segs / tseg); // tiles per stage
+        // Warps per tile: P = 1 when a stage holds at least as many tiles as warps (each warp takes
+        // whole tiles, no barrier); otherwise P warps share a tile, warp p taking segments
+        // j = p (mod P), and combine their partial updates once per stage.
+        const int P = tt_per >= kCgsWarps ? 1 : kCgsWarps / tt_per;
+        const int slot = warp / P, part = warp % P;
         const int my_tiles = a.V.ntiles > static_cast<int>(blockIdx.x)
                                  ? (a.V.ntiles - 1 - static_cast<int>(blockIdx.x)) / static_cast<int>(gridDim.x) + 1
                                  : 0;
@@ -346,57 +370,141 @@ __global__ void __launch_bounds__(kCgsThreads) cgs_pass_kernel(CgsArgs<T> a) {
             }
             asm volatile("cp.async.commit_group;\n" ::: "memory");
         };
-        __syncthreads(); // coefficients visible
+        __syncthreads(); // coefficients and accumulators visible
         for (int i = 0; i < kCgsStages; ++i)
             issue(i);
-        int flip = 0;
+        double dsq = 0; // binary32 sums of squares, exact range in binary64
+        T *myacc = accw + warp * cs;
+        // A warp owns the same segments (j = part mod P) for the whole launch: its per-lane dot
+        // partials stay in registers across tiles (fixed order) and are reduced across lanes
+        // once at the end. Shuffle-per-segment reduction is the fallback for longer sets.
+        constexpr int kOwn = 40;
+        const bool reg_dots = (kk + P - 1) / P <= kOwn;
+        T racc[kOwn];
+#pragma unroll
+        for (int i = 0; i < kOwn; ++i)
+            racc[i] = 0;
+        auto dots = [&](const T *tile, V16 cur) {
+            if (reg_dots) {
+#pragma unroll
+                for (int i0 = 0; i0 < kOwn; i0 += 8) {
+                    if (part + i0 * P >= kk)
+                        break;
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) {
+                        const int j = part + (i0 + u) * P;
+                        if (j < kk)
+                            racc[i0 + u] += VT::dot(*reinterpret_cast<const V16 *>(tile + j * R + lane * E), cur);
+                    }
+                }
+            } else {
+#pragma unroll 2
+                for (int j = part; j < kk; j += P) {
+                    T d = VT::dot(*reinterpret_cast<const V16 *>(tile + j * R + lane * E), cur);
+                    for (int o = 16; o > 0; o >>= 1)
+                        d += __shfl_xor_sync(0xffffffffu, d, o);
+                    if (lane == 0)
+                        myacc[j] += d;
+                }
+            }
+        };
         for (int item = 0; item < nitems; ++item) {
             const int st = item % kCgsStages;
             asm volatile("cp.async.wait_group %0;\n" ::"n"(kCgsStages - 1) : "memory");
             __syncthreads();
             const T *sbase = stage0 + st * stage_elems;
             const int q0 = item * tt_per;
-            const int q1 = min(my_tiles, q0 + tt_per);
-            for (int q = q0; q < q1; ++q) {
-                const int t = static_cast<int>(blockIdx.x) + q * static_cast<int>(gridDim.x);
-                const T *tile = sbase + static_cast<size_t>(q - q0) * tseg * R;
+            const int nq = min(my_tiles, q0 + tt_per) - q0;
+            // P == 1: warp takes tiles slot, slot + 8, ...; P > 1: one round, tile `slot`.
+            const int qstep = P == 1 ? kCgsWarps : nq + 1;
+            for (int qq = slot; qq < nq; qq += qstep) {
+                const int t = static_cast<int>(blockIdx.x) + (q0 + qq) * static_cast<int>(gridDim.x);
+                const T *tile = sbase + static_cast<size_t>(qq) * tseg * R;
                 V16 cur = *reinterpret_cast<const V16 *>(tile + kk * R + lane * E);
-                // Warp w owns the segments j = w (mod 8): balanced at every k, and each dot
-                // accumulator has one owner (deterministic, no atomics).
                 if (MODE >= 2) {
-                    V16 part = VT::zero();
+                    V16 acc4 = VT::zero();
 #pragma unroll 4
-                    for (int j = warp; j < kk; j += kCgsWarps)
-                        part = VT::axpy(cf[j], *reinterpret_cast<const V16 *>(tile + j * R + lane * E), part);
-                    wpart[flip][warp][lane] = part;
-                    __syncthreads();
-                    V16 tot = wpart[flip][0][lane];
-#pragma unroll
-                    for (int q2 = 1; q2 < kCgsWarps; ++q2)
-                        tot = VT::add(tot, wpart[flip][q2][lane]);
-                    cur = VT::sub(cur, tot); // pad rows: every operand is zero there
-                    if (warp == 0)
-                        *reinterpret_cast<V16 *>(a.V.seg(t, kk) + lane * E) = cur; // W_{k+1}
-                    flip ^= 1;
-                }
-                if (warp == 0)
-                    for (int e = 0; e < E; ++e)
-                        ssq_add(VT::get(cur, e));
-                if (MODE <= 2) {
-#pragma unroll 2
-                    for (int j = warp; j < kk; j += kCgsWarps) {
-                        T d = VT::dot(*reinterpret_cast<const V16 *>(tile + j * R + lane * E), cur);
-                        for (int o = 16; o > 0; o >>= 1)
-                            d += __shfl_xor_sync(0xffffffffu, d, o);
-                        if (lane == 0)
-                            acc[j] += d;
+                    for (int j = part; j < kk; j += P)
+                        acc4 = VT::axpy(cf[j], *reinterpret_cast<const V16 *>(tile + j * R + lane * E), acc4);
+                    if (P > 1) {
+                        wpart[warp][lane] = acc4; // combined after the block barrier below
+                        break;
                     }
+                    cur = VT::sub(cur, acc4); // pad rows: every operand is zero there
+                    *reinterpret_cast<V16 *>(a.V.seg(t, kk) + lane * E) = cur; // W_{k+1}
+                }
+                if (MODE <= 2)
+                    dots(tile, cur);
+                if (part == 0)
+                    for (int e = 0; e < E; ++e) {
+                        const T v = VT::get(cur, e);
+                        if (sizeof(T) == 4) {
+                            bad |= !isfinite(v);
+                            dsq += static_cast<double>(v) * static_cast<double>(v);
+                        } else {
+                            ssq_add(v);
+                        }
+                    }
+            }
+            if (P > 1 && MODE >= 2) {
+                // Combine the P partial updates of each tile in warp order, then finish the tile.
+                __syncthreads();
+                if (slot < nq) {
+                    const int qq = slot;
+                    const int t = static_cast<int>(blockIdx.x) + (q0 + qq) * static_cast<int>(gridDim.x);
+                    const T *tile = sbase + static_cast<size_t>(qq) * tseg * R;
+                    V16 tot = wpart[slot * P][lane];
+                    for (int p2 = 1; p2 < P; ++p2)
+                        tot = VT::add(tot, wpart[slot * P + p2][lane]);
+                    V16 cur = VT::sub(*reinterpret_cast<const V16 *>(tile + kk * R + lane * E), tot);
+                    if (part == 0) {
+                        *reinterpret_cast<V16 *>(a.V.seg(t, kk) + lane * E) = cur; // W_{k+1}
+                        for (int e = 0; e < E; ++e) {
+                            const T v = VT::get(cur, e);
+                            if (sizeof(T) == 4) {
+                                bad |= !isfinite(v);
+                                dsq += static_cast<double>(v) * static_cast<double>(v);
+                            } else {
+                                ssq_add(v);
+                            }
+                        }
+                    }
+                    if (MODE == 2)
+                        dots(tile, cur);
                 }
             }
             __syncthreads(); // the stage is free
             issue(item + kCgsStages);
         }
         asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+        if (MODE <= 2 && reg_dots) {
+#pragma unroll
+            for (int i = 0; i < kOwn; ++i) {
+                const int j = part + i * P;
+                if (part + i * P >= kk)
+                    break;
+                T d = racc[i];
+                for (int o = 16; o > 0; o >>= 1)
+                    d += __shfl_xor_sync(0xffffffffu, d, o);
+                if (lane == 0)
+                    myacc[j] = d;
+            }
+        }
+        __syncthreads();
+        // Per-warp accumulators -> acc in warp order (deterministic).
+        if (MODE <= 2)
+            for (int j = threadIdx.x; j < kk; j += blockDim.x) {
+                T sum = 0;
+                for (int w2 = 0; w2 < kCgsWarps; ++w2)
+                    sum += accw[w2 * cs + j];
+                acc[j] = sum;
+            }
+        if (sizeof(T) == 4 && dsq > 0) {
+            // binary64 sum of squares -> (te, ts) with ts in [1, 4)
+            const int e2 = ilogb(dsq);
+            te = e2 >= 0 ? e2 / 2 : -((1 - e2) / 2);
+            ts = static_cast<T>(ldexp(dsq, -2 * te));
+        }
     }
     for (int t = blockIdx.x; !streamed && t < a.V.ntiles; t += gridDim.x) {
         const int row0 = t * R;

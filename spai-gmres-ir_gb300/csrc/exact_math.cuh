@@ -220,27 +220,15 @@ __device__ __forceinline__ bool cr_hypot_fast(double x, double y, double &out) {
 }
 #endif
 
-// Correctly rounded (to nearest, ties to even) hypot in T = double or float.
-template <class T> SPAI_HD T cr_hypot(T a, T b) {
-    T x = std::fabs(a), y = std::fabs(b);
-    if (std::isinf(x) || std::isinf(y))
-        return T(INFINITY);
-    if (std::isnan(x) || std::isnan(y))
-        return x + y;
-    if (x < y) {
-        const T t = x;
-        x = y;
-        y = t;
-    }
-    if (y == 0)
-        return x;
-#ifdef __CUDA_ARCH__
-    {
-        T fast;
-        if (cr_hypot_fast(x, y, fast))
-            return fast;
-    }
+#ifdef __CUDACC__
+#define SPAI_HD_COLD __host__ __device__ __noinline__
+#else
+#define SPAI_HD_COLD inline
 #endif
+
+// General path for x >= y > 0 finite (out of line on the device: it runs rarely there, and
+// keeping it out of the callers keeps the fit kernels' hot code small).
+template <class T> SPAI_HD_COLD T cr_hypot_general(T x, T y) {
     const int ex = em_ilogb(x), ey = em_ilogb(y);
     // y/x below 2^-(p/2+2) with p the significand width: the exact value rounds to x.
     if (ex - ey > (sizeof(T) == 8 ? 30 : 14))
@@ -280,6 +268,30 @@ template <class T> SPAI_HD T cr_hypot(T a, T b) {
         break;
     }
     return em_ldexp(c, ex);
+}
+
+// Correctly rounded (to nearest, ties to even) hypot in T = double or float.
+template <class T> SPAI_HD T cr_hypot(T a, T b) {
+    T x = std::fabs(a), y = std::fabs(b);
+    if (std::isinf(x) || std::isinf(y))
+        return T(INFINITY);
+    if (std::isnan(x) || std::isnan(y))
+        return x + y;
+    if (x < y) {
+        const T t = x;
+        x = y;
+        y = t;
+    }
+    if (y == 0)
+        return x;
+#ifdef __CUDA_ARCH__
+    {
+        T fast;
+        if (cr_hypot_fast(x, y, fast))
+            return fast;
+    }
+#endif
+    return cr_hypot_general(x, y);
 }
 
 } // namespace spai

@@ -749,6 +749,7 @@ template <class T, class TO> struct IrEngine {
     int stage_segs = 0;   // Gram-Schmidt pipeline stage size (segments)
     size_t cgs_dyn = 0;   // dynamic shared memory of a pass
     void *cgs_dots = nullptr, *cgs_norms = nullptr;
+    T *cgs_gacc = nullptr, *cgs_gcf = nullptr; // long caps: accumulators in global memory
     bool always_reorth = false;
     int *pinned_host = nullptr; // host flag for profile-mode reads
     long long launches = 0;
@@ -909,6 +910,11 @@ template <class T, class TO> struct IrEngine {
         SPAI_CUDA(cudaMemset(V, 0, vcount * sizeof(T))); // pad rows of the last tile stay zero
         sc = arena.alloc<T>(cap + 2);
         cgs_dots = arena.alloc<T>(static_cast<size_t>(nblk_dots) * (cap + 2));
+        cgs_gacc = cgs_gcf = nullptr;
+        if (cgs_acc_global<T>(cap)) {
+            cgs_gacc = arena.alloc<T>(static_cast<size_t>(nblk_dots) * (cap + 2));
+            cgs_gcf = arena.alloc<T>(static_cast<size_t>(nblk_dots) * (cap + 2));
+        }
         cgs_norms = arena.alloc<Ssq<T>>(nblk_dots);
         const int smem = static_cast<int>(cgs_dyn);
         SPAI_CUDA(cudaFuncSetAttribute(cgs_pass_kernel<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
@@ -950,7 +956,7 @@ template <class T, class TO> struct IrEngine {
     CgsArgs<T> cgs_args() const {
         return CgsArgs<T>{n, basis(), w, h1, h2, H, cs, sn, g, sc, hld, ctl,
                           CgsScratch{cgs_dots, cgs_norms, counters + kSlotDots}, always_reorth ? 1 : 0,
-                          stage_segs};
+                          stage_segs, cgs_gacc, cgs_gcf};
     }
     size_t cgs_smem() const {
         return cgs_dyn;

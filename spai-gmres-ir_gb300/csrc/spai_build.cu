@@ -265,9 +265,19 @@ template <class T> struct ColumnArgs {
     T *packed_val;
     unsigned long long *packed_top;
     unsigned long long packed_cap;
-    int *queue;        // [0] next column, [1] list-1 size, [2] next in list 1, [3] list-2 size, [4] next in list 2
-    int *overflow_list, *overflow_list2;
     int *error;        // bit0 packed output full, bit1 column exceeded the largest workspace
+};
+
+// Columns one launch of the column kernel takes, and where its misfits go. Workspace tiers form a
+// chain: the first launch takes every column; each later launch takes the previous launch's
+// misfits with a larger workspace per group; the last (global-memory) tier has no out list, so a
+// misfit there is an error.
+struct TierIo {
+    const int *in_list;  // nullptr: columns 0..n-1
+    const int *in_count; // size of in_list (device)
+    int *next;           // take counter
+    int *out_list;       // misfits (nullptr: error)
+    int *out_count;
 };
 
 // Gather the dense reduced matrix R = B(I, J) (row-major m x q): R[i*q+jj] = A(J[jj], I[i]) d_J.
@@ -814,48 +824,31 @@ __device__ int fit_column(const Grp &g, const ColumnArgs<T> &A, int k, char *ws,
     return status;
 }
 
-// Persistent column kernel with G lanes per column (32/G columns per warp). mode 0: all columns
-// via the atomic queue, shared-memory workspace of ws_bytes per group; columns that do not fit go
-// to the overflow list. mode 1: the overflow list, global workspace gws of ws_bytes per group.
+// Persistent column kernel with G lanes per column (32/G columns per warp): groups take columns
+// from io (all columns, or the previous tier's misfits) with a workspace of ws_bytes per group in
+// shared memory (gws == nullptr) or in global memory (gws + group * ws_bytes).
 template <class T, int G, bool FAST>
-__global__ void spai_columns_kernel(ColumnArgs<T> A, int mode, size_t ws_bytes, int qcap,
-                                    char *gws) {
-    // mode 0: all columns from queue[0], shared workspace ws_bytes per group; misfits -> list 1.
-    // mode 2: list 1 from queue[2], one group per block using the block's shared memory; misfits
-    //         -> list 2 (queue[3]).
-    // mode 3: list 2 from queue[4], global workspace ws_bytes per group; misfits -> error.
+__global__ void __launch_bounds__(sizeof(T) == 8 ? 512 : 768)
+    spai_columns_kernel(ColumnArgs<T> A, TierIo io, size_t ws_bytes, int qcap, char *gws) {
     extern __shared__ __align__(16) char smem[];
     const auto g = cg::tiled_partition<G>(cg::this_thread_block());
     const int grp = threadIdx.x / G;
     const int ggrp = (blockIdx.x * blockDim.x + threadIdx.x) / G;
-    char *ws = mode == 3 ? gws + static_cast<size_t>(ggrp) * ws_bytes
-                         : smem + static_cast<size_t>(grp) * ws_bytes;
+    char *ws = gws ? gws + static_cast<size_t>(ggrp) * ws_bytes : smem + static_cast<size_t>(grp) * ws_bytes;
     const int lane = g.thread_rank();
+    const int total = io.in_list ? *io.in_count : A.n;
     for (;;) {
         int slot = 0;
         if (lane == 0)
-            slot = atomicAdd(mode == 0 ? &A.queue[0] : (mode == 2 ? &A.queue[2] : &A.queue[4]), 1);
+            slot = atomicAdd(io.next, 1);
         slot = g.shfl(slot, 0);
-        int k;
-        if (mode == 0) {
-            if (slot >= A.n)
-                break;
-            k = slot;
-        } else if (mode == 2) {
-            if (slot >= A.queue[1])
-                break;
-            k = A.overflow_list[slot];
-        } else {
-            if (slot >= A.queue[3])
-                break;
-            k = A.overflow_list2[slot];
-        }
+        if (slot >= total)
+            break;
+        const int k = io.in_list ? io.in_list[slot] : slot;
         const int r = fit_column<FAST>(g, A, k, ws, ws_bytes, qcap);
         if (r == kOverflow && lane == 0) {
-            if (mode == 0)
-                A.overflow_list[atomicAdd(&A.queue[1], 1)] = k;
-            else if (mode == 2)
-                A.overflow_list2[atomicAdd(&A.queue[3], 1)] = k;
+            if (io.out_list)
+                io.out_list[atomicAdd(io.out_count, 1)] = k;
             else
                 atomicOr(A.error, 2);
         }
@@ -923,56 +916,91 @@ __global__ void stats_kernel(int n, const int *__restrict__ fits, const int *__r
 // ------------------------------------------------------------------------------------------
 // Host driver.
 // ------------------------------------------------------------------------------------------
-// Launch the column kernel for a group width G: `work` groups of G lanes in blocks of `threads`.
-// mode 0 sizes the grid to the SMs' resident capacity (persistent); mode 1 launches one block
-// per `per_block` groups.
+// Launch the column kernel for a group width G with `threads` per block: persistent over the
+// SMs (shared-memory workspace, at most max_blocks blocks) or exactly max_blocks blocks (global).
 template <class T, int G, bool FAST>
-void launch_columns_g(ColumnArgs<T> args, int mode, size_t ws, int qcap, char *gws, size_t smem,
-                      int threads, long long work, int groups_per_block, int sms, cudaStream_t st) {
-    if (mode != 3) {
-        SPAI_CUDA(cudaFuncSetAttribute(spai_columns_kernel<T, G, FAST>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+void launch_columns_g(ColumnArgs<T> args, TierIo io, size_t ws, int qcap, char *gws, int threads,
+                      long long max_blocks, int sms, cudaStream_t st) {
+    long long blocks = max_blocks;
+    size_t smem = 0;
+    if (!gws) {
+        smem = ws * static_cast<size_t>(threads / G);
+        SPAI_CUDA(cudaFuncSetAttribute(spai_columns_kernel<T, G, FAST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        static_cast<int>(smem)));
         int per_sm = 0;
-        SPAI_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, spai_columns_kernel<T, G, FAST>,
-                                                                threads, smem));
-        if (per_sm < 1)
-            per_sm = 1;
-        const long long needed = (work + groups_per_block - 1) / groups_per_block;
-        const unsigned blocks = static_cast<unsigned>(
-            std::max<long long>(1, std::min<long long>(needed, static_cast<long long>(sms) * per_sm)));
-        spai_columns_kernel<T, G, FAST><<<blocks, threads, smem, st>>>(args, mode, ws, qcap, nullptr);
-    } else {
-        const unsigned blocks = static_cast<unsigned>((work + groups_per_block - 1) / groups_per_block);
-        spai_columns_kernel<T, G, FAST><<<blocks, threads, 0, st>>>(args, 3, ws, qcap, gws);
+        SPAI_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, spai_columns_kernel<T, G, FAST>, threads, smem));
+        blocks = std::min<long long>(max_blocks, static_cast<long long>(sms) * std::max(per_sm, 1));
     }
+    spai_columns_kernel<T, G, FAST><<<static_cast<unsigned>(std::max<long long>(blocks, 1)), threads, smem, st>>>(
+        args, io, ws, qcap, gws);
     SPAI_LAUNCH("spai_columns_kernel");
 }
 template <class T, bool FAST>
-void launch_columns_f(int G, ColumnArgs<T> args, int mode, size_t ws, int qcap, char *gws, size_t smem,
-                      int threads, long long work, int groups_per_block, int sms, cudaStream_t st) {
+void launch_columns_f(int G, ColumnArgs<T> args, TierIo io, size_t ws, int qcap, char *gws, int threads,
+                      long long max_blocks, int sms, cudaStream_t st) {
     switch (G) {
     case 4:
-        launch_columns_g<T, 4, FAST>(args, mode, ws, qcap, gws, smem, threads, work, groups_per_block, sms, st);
+        launch_columns_g<T, 4, FAST>(args, io, ws, qcap, gws, threads, max_blocks, sms, st);
         break;
     case 8:
-        launch_columns_g<T, 8, FAST>(args, mode, ws, qcap, gws, smem, threads, work, groups_per_block, sms, st);
+        launch_columns_g<T, 8, FAST>(args, io, ws, qcap, gws, threads, max_blocks, sms, st);
         break;
     case 16:
-        launch_columns_g<T, 16, FAST>(args, mode, ws, qcap, gws, smem, threads, work, groups_per_block, sms, st);
+        launch_columns_g<T, 16, FAST>(args, io, ws, qcap, gws, threads, max_blocks, sms, st);
         break;
     default:
-        launch_columns_g<T, 32, FAST>(args, mode, ws, qcap, gws, smem, threads, work, groups_per_block, sms, st);
+        launch_columns_g<T, 32, FAST>(args, io, ws, qcap, gws, threads, max_blocks, sms, st);
     }
 }
 template <class T>
-void launch_columns(bool fast, int G, ColumnArgs<T> args, int mode, size_t ws, int qcap, char *gws,
-                    size_t smem, int threads, long long work, int groups_per_block, int sms,
-                    cudaStream_t st) {
+void launch_columns(bool fast, int G, ColumnArgs<T> args, TierIo io, size_t ws, int qcap, char *gws, int threads,
+                    long long max_blocks, int sms, cudaStream_t st) {
     if (fast)
-        launch_columns_f<T, true>(G, args, mode, ws, qcap, gws, smem, threads, work, groups_per_block, sms, st);
+        launch_columns_f<T, true>(G, args, io, ws, qcap, gws, threads, max_blocks, sms, st);
     else
-        launch_columns_f<T, false>(G, args, mode, ws, qcap, gws, smem, threads, work, groups_per_block, sms, st);
+        launch_columns_f<T, false>(G, args, io, ws, qcap, gws, threads, max_blocks, sms, st);
+}
+
+// One workspace tier: group width, bytes per group, groups per block, pattern capacity, and
+// whether the workspace is in global memory.
+struct TierPlan {
+    int G;
+    size_t ws;
+    int groups_per_block;
+    int qcap;
+    bool global;
+};
+
+// Tier chain from the sparsity profile: shared-memory workspaces doubling from the profile's
+// first size while at least four groups still fit on an SM, then global-memory workspaces (1 MiB
+// for 16 groups per SM, then 32 MiB). Keeping many groups resident matters more than where the
+// workspace lives: a fit is a chain of dependent shared/global accesses, and with one group per
+// SM every latency is exposed (measured on the 10^6 irregular system: a 224 KiB shared tier fitted
+// about 1,300 columns/s, the 1 MiB global tier about 2,900 columns/s on larger columns). Columns
+// that do not fit move up the chain and are fitted again from the start (fits are deterministic,
+// so the result does not depend on the tier that completes a column).
+inline std::vector<TierPlan> plan_tiers(size_t first_ws, int first_G, int max_threads, size_t smem_budget) {
+    std::vector<TierPlan> tiers;
+    auto qcap_for = [](size_t ws) {
+        return ws <= 4096 ? 32 : (ws <= 16384 ? 64 : (ws <= 65536 ? 256 : 1024));
+    };
+    const size_t last_shared = smem_budget / 4;
+    size_t ws = first_ws;
+    int G = first_G;
+    while (ws <= std::max(last_shared, first_ws)) {
+        const int per_warp = 32 / G;
+        int groups = static_cast<int>(std::min<size_t>(smem_budget / ws, static_cast<size_t>(max_threads / G)));
+        groups = std::max(per_warp, (groups / per_warp) * per_warp);
+        if (static_cast<size_t>(groups) * ws > smem_budget)
+            break;
+        tiers.push_back(TierPlan{G, ws, groups, qcap_for(ws), false});
+        ws *= 2;
+        if (ws > 16384)
+            G = std::max(G, 16);
+    }
+    tiers.push_back(TierPlan{32, size_t(1) << 20, 4, 4096, true});   // 1 MiB, 16 groups per SM
+    tiers.push_back(TierPlan{32, size_t(32) << 20, 1, 65536, true}); // 32 MiB, at most 512 groups
+    return tiers;
 }
 
 template <class T>
@@ -1024,7 +1052,7 @@ void SpaiBuilder<T>::construct(const DeviceCsr<T> &a, const SpaiParams &prm, cud
     out.col_q = arena.alloc<int>(n);
     out.col_residual = arena.alloc<T>(n);
     long long *off = arena.alloc<long long>(n);
-    int *queue = arena.alloc<int>(8);
+    int *queue = arena.alloc<int>(64);
     int *err = arena.alloc<int>(1);
     unsigned long long *top = arena.alloc<unsigned long long>(1);
     int *ovl = arena.alloc<int>(n);
@@ -1036,82 +1064,73 @@ void SpaiBuilder<T>::construct(const DeviceCsr<T> &a, const SpaiParams &prm, cud
     // sets): short-row matrices (stencils) use many small workspaces; heavy-tailed rows use
     // fewer, larger ones. Overrides come from SpaiParams.
     const bool heavy = a.max_row > 48 || static_cast<double>(nnz) > 12.0 * n;
-    const int G = prm.group_lanes > 0 ? prm.group_lanes : (heavy ? 16 : 8);
+    const int G0 = prm.group_lanes > 0 ? prm.group_lanes : (heavy ? 16 : 8);
     const int ws_default = heavy ? 28672 : (sizeof(T) == 8 ? 12288 : 6144);
-    const int ws_bytes = prm.ws_bytes_per_warp > 0 ? prm.ws_bytes_per_warp : ws_default;
-    const int per_warp = 32 / G;
-    const int smem_budget = 225 * 1024;
-    // Groups per block: fill one SM's shared memory, within the register budget of one block
-    // (124 registers/thread for binary64, 77 for binary32 -> at most 512 / 768 threads), in
-    // whole warps.
+    const size_t ws0 = prm.ws_bytes_per_warp > 0 ? prm.ws_bytes_per_warp : ws_default;
+    const size_t smem_budget = 225 * 1024;
+    // Threads per block within the register budget of one block (124 registers/thread for
+    // binary64, 77 for binary32 -> at most 512 / 768 threads).
     const int max_threads = sizeof(T) == 8 ? 512 : 768;
-    int groups = prm.warps_per_block > 0 ? prm.warps_per_block * per_warp : smem_budget / ws_bytes;
-    groups = std::min(groups, max_threads / G);
-    groups = std::max(per_warp, (groups / per_warp) * per_warp);
-    if (static_cast<long long>(groups) * ws_bytes > smem_budget)
+    if (ws0 > smem_budget)
         throw ArgumentError("SPAI workspace per group too large for one block's shared memory");
-    const int threads = ((groups * G + 31) / 32) * 32;
-    const int groups_launched = threads / G;
-    const int qcap_main = 64;
-    out.group_lanes = G;
-    out.ws_bytes = ws_bytes;
-    // SPAI_TRACE=1 prints the wall time of each workspace tier to stderr (tuning aid).
+    const std::vector<TierPlan> tiers = plan_tiers(ws0, G0, max_threads, smem_budget);
+    out.group_lanes = tiers[0].G;
+    out.ws_bytes = static_cast<int>(tiers[0].ws);
+    int sms = 0, dev = 0;
+    SPAI_CUDA(cudaGetDevice(&dev));
+    SPAI_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    // SPAI_TRACE=1 prints the wall time and misfit count of each workspace tier to stderr.
     const bool trace = std::getenv("SPAI_TRACE") != nullptr;
     auto clock_ms = [] {
         return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
     };
-    double t_tier = clock_ms();
     for (int attempt = 0;; ++attempt) {
         pidx = arena.alloc<int>(cap);
         pv = arena.alloc<T>(cap);
-        SPAI_CUDA(cudaMemsetAsync(queue, 0, sizeof(int) * 8, st));
+        SPAI_CUDA(cudaMemsetAsync(queue, 0, sizeof(int) * 64, st));
         SPAI_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
         SPAI_CUDA(cudaMemsetAsync(top, 0, sizeof(unsigned long long), st));
         ColumnArgs<T> args{n, a.rp, a.ci, a.val, tp, ti, d, static_cast<T>(prm.epsilon), prm.alpha,
                            prm.beta, out.col_status, out.col_fits, out.col_growths, out.col_clamps,
-                           out.col_q, out.col_residual, off, pidx, pv, top, cap, queue, ovl, ovl2, err};
-        const size_t smem = static_cast<size_t>(ws_bytes) * groups_launched;
-        int sms = 0, dev = 0;
-        SPAI_CUDA(cudaGetDevice(&dev));
-        SPAI_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-        launch_columns<T>(prm.fast, G, args, 0, ws_bytes, qcap_main, nullptr, smem, threads, n, groups_launched,
-                          sms, st);
-        ++out.launches;
-        int h_queue[8];
-        SPAI_CUDA(cudaMemcpyAsync(h_queue, queue, sizeof(h_queue), cudaMemcpyDeviceToHost, st));
-        SPAI_CUDA(cudaStreamSynchronize(st));
-        out.overflow_columns = h_queue[1];
-        if (trace) {
-            std::fprintf(stderr, "spai main tier: G=%d ws=%d groups/block=%d  %.1f ms, overflow %d\n", G, ws_bytes,
-                         groups_launched, clock_ms() - t_tier, h_queue[1]);
-            t_tier = clock_ms();
-        }
-        if (h_queue[1] > 0) {
-            // Tier 2: one 32-lane group per block with the whole shared memory of an SM. Columns
-            // that still do not fit are listed again (queue[3]) for tier 3.
-            const size_t big = static_cast<size_t>(smem_budget);
-            launch_columns<T>(prm.fast, 32, args, 2, big, 1024, nullptr, big, 32, std::min(h_queue[1], sms), 1,
-                              sms, st);
+                           out.col_q, out.col_residual, off, pidx, pv, top, cap, err};
+        out.overflow_columns = 0;
+        out.overflow_columns_global = 0;
+        int pending = n;          // columns the next tier takes
+        const int *in_list = nullptr;
+        int *lists[2] = {ovl, ovl2};
+        for (size_t ti_ = 0; ti_ < tiers.size() && pending > 0; ++ti_) {
+            const TierPlan &tp_ = tiers[ti_];
+            const bool last = ti_ + 1 == tiers.size();
+            int *out_list = last ? nullptr : lists[ti_ & 1];
+            TierIo io{in_list, ti_ == 0 ? nullptr : &queue[2 * ti_ - 1], &queue[2 * ti_], out_list,
+                      &queue[2 * ti_ + 1]};
+            const double t0 = trace ? clock_ms() : 0.0;
+            const int threads = ((tp_.groups_per_block * tp_.G + 31) / 32) * 32;
+            char *gws = nullptr;
+            long long blocks = (static_cast<long long>(pending) + tp_.groups_per_block - 1) / tp_.groups_per_block;
+            if (tp_.global) {
+                const long long groups = std::min<long long>(pending, ti_ + 2 == tiers.size() ? sms * 16LL : 512LL);
+                blocks = (groups + tp_.groups_per_block - 1) / tp_.groups_per_block;
+                // one workspace for every launched group (blocks * groups_per_block >= groups)
+                gws = arena.alloc<char>(tp_.ws * static_cast<size_t>(blocks * tp_.groups_per_block));
+                if (out.overflow_columns_global == 0)
+                    out.overflow_columns_global = pending;
+            }
+            launch_columns<T>(prm.fast, tp_.G, args, io, tp_.ws, tp_.qcap, gws, threads, blocks, sms, st);
             ++out.launches;
-            SPAI_CUDA(cudaMemcpyAsync(h_queue, queue, sizeof(h_queue), cudaMemcpyDeviceToHost, st));
+            int h_next = 0;
+            if (!last) {
+                SPAI_CUDA(cudaMemcpyAsync(&h_next, &queue[2 * ti_ + 1], sizeof(int), cudaMemcpyDeviceToHost, st));
+            }
             SPAI_CUDA(cudaStreamSynchronize(st));
-            out.overflow_columns_global = h_queue[3];
-            if (trace) {
-                std::fprintf(stderr, "spai shared tier: %.1f ms, to global %d\n", clock_ms() - t_tier, h_queue[3]);
-                t_tier = clock_ms();
-            }
-        }
-        if (h_queue[3] > 0) {
-            // Tier 3: global-memory workspace per 32-lane group.
-            const size_t gws_bytes = prm.overflow_ws_bytes > 0 ? prm.overflow_ws_bytes : (size_t(32) << 20);
-            const int og = std::min(h_queue[3], 512);
-            char *gws = arena.alloc<char>(gws_bytes * og);
-            launch_columns<T>(prm.fast, 32, args, 3, gws_bytes, 65536, gws, 0, 32, og, 1, sms, st);
-            ++out.launches;
-            if (trace) {
-                SPAI_CUDA(cudaStreamSynchronize(st));
-                std::fprintf(stderr, "spai global tier: %.1f ms (%d groups)\n", clock_ms() - t_tier, og);
-            }
+            if (trace)
+                std::fprintf(stderr, "spai tier %zu: G=%d ws=%zu%s groups/block=%d columns=%d  %.1f ms, misfits %d\n", ti_,
+                             tp_.G, tp_.ws, tp_.global ? " (global)" : "", tp_.groups_per_block, pending,
+                             clock_ms() - t0, h_next);
+            if (ti_ == 0)
+                out.overflow_columns = h_next;
+            pending = h_next;
+            in_list = out_list;
         }
         int h_err = 0;
         SPAI_CUDA(cudaMemcpyAsync(&h_err, err, sizeof(int), cudaMemcpyDeviceToHost, st));
