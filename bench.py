@@ -49,7 +49,7 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batched", action="store_true",
                     help="skip the batched-systems line (512 independent 2-D systems in one call)")
-    ap.add_argument("--profile-run", choices=["mixed", "f64"], default=None,
+    ap.add_argument("--profile-run", choices=["mixed", "f64", "batched", "gmres"], default=None,
                     help="one untimed build+solve of the workload (a clean launch sequence for ncu)")
     ap.add_argument("--no-graph", action="store_true",
                     help="profile run: drive the refinement loop from the host instead of one CUDA graph "
@@ -60,6 +60,25 @@ def parse():
 def profile_run(args):
     import spai_ir
     from spai_ir import matrices as M
+
+    if args.profile_run == "gmres":
+        # one binary32 GMRES run of exactly --innercap Arnoldi steps (tau = 1e-30 never accepts):
+        # every launch of step k has known algorithmic bytes (traffic captures)
+        system = M.convection_diffusion_3d(args.grid)
+        n = system[0]
+        with spai_ir.Handle(system, "mixed") as h:
+            h.build(spai_ir.cli_options(n, "mixed"))
+            x, r = h.gmres(M.equal_rhs(n), 1e-30, args.innercap)
+        print(json.dumps({"profile_run": "gmres", "n": n, "steps": r["iterations"], "status": r["status"]}))
+        return
+    if args.profile_run == "batched":
+        # --grid is the number of systems here (sides log-uniform in [32, 256])
+        systems = M.batched_convection_diffusion(args.grid, seed=0)
+        opts = spai_ir.options("mixed", epsilon=0.3, alpha=5, innercap=100)
+        xs, reps = spai_ir.ir_solve_batched(systems, [M.equal_rhs(s[0]) for s in systems], opts)
+        print(json.dumps({"profile_run": "batched", "systems": len(systems), "spai_ms": reps[0]["spai_ms"],
+                          "solve_ms": reps[0]["solve_ms"], "converged": sum(r["converged"] for r in reps)}))
+        return
 
     system = M.convection_diffusion_3d(args.grid)
     n = system[0]
@@ -246,10 +265,12 @@ def run_ours(args, rank, world, local):
     peak, peak_kind = measured_peaks()
     d = prof[dom]
     achieved = d["bytes"] / (d["ms"] * 1e-3) / 1e9 if d["ms"] > 0 else 0.0
+    # DRAM bytes per launch: the ncu-measured traffic/algorithmic ratio of this kernel class (a
+    # capture at a known Arnoldi step, profiles/) times this run's algorithmic bytes per launch.
     traffic = None
     tr = profile_traffic()
-    if tr and tr.get("kernel_class") == dom:
-        traffic = tr.get("dram_bytes_per_launch")
+    if tr and tr.get("kernel_class") == dom and tr.get("traffic_over_algorithmic"):
+        traffic = round(float(tr["traffic_over_algorithmic"]) * d["bytes"] / max(d["launches"], 1))
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "traffic": traffic, "kernel": dom,
                 "peak_source": peak_kind,
