@@ -384,8 +384,43 @@ __global__ void __launch_bounds__(kCgsThreads) cgs_pass_kernel(CgsArgs<T> a) {
 #pragma unroll
         for (int i = 0; i < kOwn; ++i)
             racc[i] = 0;
+        // Pass 2 keeps a warp's segments in registers between the update and the second dot
+        // products when it owns few enough of them (one shared-memory read of the tile, not two).
+        constexpr int kCache = sizeof(T) == 4 ? 26 : 12;
+        const bool cache = MODE == 2 && (kk + P - 1) / P <= kCache;
+        V16 vr[kCache];
+        auto update_part = [&](const T *tile) {
+            V16 acc4 = VT::zero();
+            if (cache) {
+#pragma unroll
+                for (int i0 = 0; i0 < kCache; i0 += 2) {
+                    if (part + i0 * P >= kk)
+                        break;
+#pragma unroll
+                    for (int u = 0; u < 2; ++u) {
+                        const int i = i0 + u, j = part + i * P;
+                        if (i < kCache && j < kk) {
+                            vr[i] = *reinterpret_cast<const V16 *>(tile + j * R + lane * E);
+                            acc4 = VT::axpy(cf[j], vr[i], acc4);
+                        }
+                    }
+                }
+            } else {
+#pragma unroll 4
+                for (int j = part; j < kk; j += P)
+                    acc4 = VT::axpy(cf[j], *reinterpret_cast<const V16 *>(tile + j * R + lane * E), acc4);
+            }
+            return acc4;
+        };
         auto dots = [&](const T *tile, V16 cur) {
-            if (reg_dots) {
+            if (cache) {
+#pragma unroll
+                for (int i = 0; i < kCache; ++i) {
+                    if (part + i * P >= kk)
+                        break;
+                    racc[i] += VT::dot(vr[i], cur);
+                }
+            } else if (reg_dots) {
 #pragma unroll
                 for (int i0 = 0; i0 < kOwn; i0 += 8) {
                     if (part + i0 * P >= kk)
@@ -422,10 +457,7 @@ __global__ void __launch_bounds__(kCgsThreads) cgs_pass_kernel(CgsArgs<T> a) {
                 const T *tile = sbase + static_cast<size_t>(qq) * tseg * R;
                 V16 cur = *reinterpret_cast<const V16 *>(tile + kk * R + lane * E);
                 if (MODE >= 2) {
-                    V16 acc4 = VT::zero();
-#pragma unroll 4
-                    for (int j = part; j < kk; j += P)
-                        acc4 = VT::axpy(cf[j], *reinterpret_cast<const V16 *>(tile + j * R + lane * E), acc4);
+                    const V16 acc4 = update_part(tile);
                     if (P > 1) {
                         wpart[warp][lane] = acc4; // combined after the block barrier below
                         break;

@@ -103,14 +103,23 @@ __device__ __forceinline__ void sell_rows(const DeviceSell<T> &m, XF xget, T sca
         const int l = m.len[row];
         T acc = 0;
         int p = 0;
-        for (; p + 2 <= l; p += 2) {
-            const int c0 = __ldg(m.ci + base + 32LL * p), c1 = __ldg(m.ci + base + 32LL * (p + 1));
-            const T v0 = __ldg(m.val + base + 32LL * p), v1 = __ldg(m.val + base + 32LL * (p + 1));
-            const T x0 = xget(c0), x1 = xget(c1);
-            acc += v0 * x0;
-            acc += v1 * x1;
+        // Four entries in flight per thread (indices and values first, then the gathers).
+        for (; p + 4 <= l; p += 4) {
+            int c[4];
+            T v[4], x[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                c[u] = __ldg(m.ci + base + 32LL * (p + u));
+                v[u] = __ldg(m.val + base + 32LL * (p + u));
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                x[u] = xget(c[u]);
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                acc += v[u] * x[u];
         }
-        if (p < l)
+        for (; p < l; ++p)
             acc += __ldg(m.val + base + 32LL * p) * xget(__ldg(m.ci + base + 32LL * p));
         y[row] = acc * scale;
     }
