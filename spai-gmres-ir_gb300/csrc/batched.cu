@@ -341,7 +341,10 @@ __device__ void ir_residual(const BatchArgs &a, const BatchSys &d, St &s, const 
             rinf = fmax(rinf, fabs(res));
             xinf = fmax(xinf, fabs(x[row]));
             const double cden = fabs(b[row]) + absacc;
-            cbe = fmax(cbe, cden == 0 ? (res == 0 ? 0.0 : INFINITY) : fabs(res) / cden);
+            if (cden == 0)
+                cbe = fmax(cbe, res == 0 ? 0.0 : INFINITY);
+            else if (fabs(res) >= cbe * cden * 0.99999999999999911182) // divide only when it can win
+                cbe = fmax(cbe, fabs(res) / cden);
         }
     }
     bad = __syncthreads_or(bad);

@@ -422,9 +422,14 @@ __global__ void __launch_bounds__(kBlock) ir_residual_kernel(int n, const int *_
             rinf = fmax(rinf, static_cast<double>(fabs(res)));
             xinf = fmax(xinf, static_cast<double>(fabs(x[row])));
             const double cden = static_cast<double>(fabs(b[row]) + absacc);
-            const double ratio = cden == 0 ? (res == TO(0) ? 0.0 : INFINITY)
-                                           : static_cast<double>(fabs(res)) / cden;
-            cbe = fmax(cbe, ratio);
+            const double ares = static_cast<double>(fabs(res));
+            // Divide only when this row's ratio can exceed the running maximum (the guard errs
+            // low by 2^-50, so the result is the maximum of the rounded ratios exactly); the
+            // binary64 division is the expensive part of this kernel on GB300's binary64 pipe.
+            if (cden == 0)
+                cbe = fmax(cbe, res == TO(0) ? 0.0 : INFINITY);
+            else if (ares >= cbe * cden * 0.99999999999999911182)
+                cbe = fmax(cbe, ares / cden);
         }
     }
     rinf = block_reduce_max(rinf, sh);
