@@ -83,10 +83,36 @@ enum { SPAI_PREC_F64 = 0, SPAI_PREC_F32 = 1, SPAI_PREC_MIXED = 2 };
 /* Option flags. */
 enum {
     SPAI_FLAG_NO_GRAPH = 1,  /* run the refinement loop with host launches instead of one graph */
-    SPAI_FLAG_FAST_SPAI = 2  /* build the SPAI with group-parallel norms, a parallel mean and hashed
+    SPAI_FLAG_FAST_SPAI = 2, /* build the SPAI with group-parallel norms, a parallel mean and hashed
                                 candidate sets instead of the reference's sequential arithmetic
                                 (patterns may differ on near-tied scores; not bit-reproducible) */
+    SPAI_FLAG_HISTORY = 4    /* record the refinement history of the solve (spai_history) */
 };
+
+/* Refinement history of one solve (IrResult::history / inner_history / update_applied and
+ * GmresResult::history, ir.hpp:26-56, gmres.hpp:28-50), recorded on the device when the solve
+ * ran with SPAI_FLAG_HISTORY. */
+typedef struct {
+    int64_t step;               /* 0 = x0 = P b, then one record per applied correction */
+    double residual_inf, residual_2;
+    double normwise_backward_error, componentwise_backward_error;
+} spai_outer_record;
+typedef struct {
+    int32_t status;             /* GMRES_* */
+    int32_t update_applied;     /* the correction was added and its iterate evaluated */
+    int64_t iterations;
+    double final_relative;      /* last recomputed preconditioned relative residual (NaN: none) */
+} spai_inner_record;
+typedef struct {
+    int64_t inner;              /* 1-based inner solve */
+    int64_t iteration;          /* 1-based Arnoldi step */
+    double estimated_relative;  /* |g_{k+1}| / ||P rhs|| after the Givens update */
+    double recomputed_relative; /* verified candidate's relative residual; NaN when the step was
+                                   not verified (candidates are formed only when the acceptance
+                                   rule can accept them) */
+    int32_t accepted;
+    int32_t pad;
+} spai_iteration_record;
 
 /* Canonical CSR on the host (row_offsets[n+1], sorted col_indices[nnz], no stored zeros), the
  * layout of CsrMatrix (include/bspai/cpu.hpp:17-43) with 64-bit indices. */
@@ -209,6 +235,14 @@ int spai_adjoint(spai_handle *h, int64_t nrhs, const double *x, const double *dL
 int spai_adjoint_device(spai_handle *h, int64_t nrhs, const double *d_x, const double *d_dLdx,
                         double *d_dLdb, double *d_dLdA_values, const spai_options *opt,
                         spai_report *rep);
+
+/* History of the handle's last solve that ran with SPAI_FLAG_HISTORY: copies at most max_* records
+ * of each kind and reports the recorded counts (n_* may exceed max_*; iteration records stop at
+ * 1,048,576). Any output pointer may be NULL. No counterpart in the reference's C++ API beyond
+ * the IrResult/GmresResult histories it returns (ir.hpp:44-56). */
+int spai_history(spai_handle *h, spai_outer_record *outer, int64_t max_outer, int64_t *n_outer,
+                 spai_inner_record *inner, int64_t max_inner, int64_t *n_inner,
+                 spai_iteration_record *iterations, int64_t max_iterations, int64_t *n_iterations);
 
 /* Per-kernel-class timing of refinement solves (CUDA events on the handle's stream around each
  * launch). Classes: 0 SpMV with A (basis vector gathered), 1 SpMV with P, 2 Gram-Schmidt pass 1

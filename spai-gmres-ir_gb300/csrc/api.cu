@@ -121,6 +121,12 @@ struct spai_handle_s {
     IrEngine<float, double> jmix;
     IrEngine<float, float> j32;
     int adj_cap = -1;
+    // History of the last solve run with SPAI_FLAG_HISTORY (device records + counts).
+    const spai_outer_record *hist_outer = nullptr;
+    const spai_inner_record *hist_inner = nullptr;
+    const spai_iteration_record *hist_iter = nullptr;
+    int hist_n_outer = 0, hist_n_inner = 0, hist_n_iter = 0;
+    int hist_cap_outer = 0, hist_cap_inner = 0, hist_cap_iter = 0;
     KernelProfile prof;
     double spai_ms = 0;
     long long spai_launches = 0;
@@ -257,6 +263,20 @@ void ensure_adjoint(spai_handle *h, int cap) {
 }
 
 // One refinement solve on the engine of the handle's precision; b, x device binary64 vectors.
+template <class E> void keep_history(spai_handle *h, const E &e, const Ctl &c, const SolveSettings &s) {
+    if (!s.history)
+        return;
+    h->hist_outer = e.hist_outer;
+    h->hist_inner = e.hist_inner;
+    h->hist_iter = e.hist_iter;
+    h->hist_cap_outer = e.hist_cap_outer;
+    h->hist_cap_inner = e.hist_cap_inner;
+    h->hist_cap_iter = e.hist_cap_iter;
+    h->hist_n_outer = c.h_n_outer;
+    h->hist_n_inner = c.h_n_inner;
+    h->hist_n_iter = c.h_n_iter;
+}
+
 template <class E64, class EMX, class E32>
 void run_solve(spai_handle *h, E64 &e64, EMX &emix, E32 &e32, const double *d_b, double *d_x,
                const SolveSettings &s, spai_report *rep) {
@@ -266,11 +286,13 @@ void run_solve(spai_handle *h, E64 &e64, EMX &emix, E32 &e32, const double *d_b,
         e64.solve(h->stream, d_b, d_x, s, h->pinned);
         rep->solve_ms = timer.stop();
         read_ctl(h, e64, c);
+        keep_history(h, e64, c, s);
         rep->kernel_launches = e64.graph_mode ? e64.graph_kernels(c) : e64.launches;
     } else if (h->precision == SPAI_PREC_MIXED) {
         emix.solve(h->stream, d_b, d_x, s, h->pinned);
         rep->solve_ms = timer.stop();
         read_ctl(h, emix, c);
+        keep_history(h, emix, c, s);
         rep->kernel_launches = emix.graph_mode ? emix.graph_kernels(c) : emix.launches;
     } else {
         // binary32 drop-in: b rounded to binary32, refinement in binary32.
@@ -284,6 +306,7 @@ void run_solve(spai_handle *h, E64 &e64, EMX &emix, E32 &e32, const double *d_b,
         SPAI_LAUNCH("convert_kernel");
         rep->solve_ms = timer.stop();
         read_ctl(h, e32, c);
+        keep_history(h, e32, c, s);
         rep->kernel_launches = (e32.graph_mode ? e32.graph_kernels(c) : e32.launches) + 2;
     }
     fill_from_ctl(c, rep);
@@ -298,6 +321,7 @@ SolveSettings settings_for(const spai_handle *h, const spai_options &o, int cap)
     s.scale_rhs = h->precision == SPAI_PREC_MIXED;
     s.accept_every = h->precision == SPAI_PREC_F32;
     s.use_graph = (o.flags & SPAI_FLAG_NO_GRAPH) == 0;
+    s.history = (o.flags & SPAI_FLAG_HISTORY) != 0;
     return s;
 }
 
@@ -522,6 +546,8 @@ int spai_build(spai_handle *h, const spai_options *opt, spai_report *rep) {
         prm.group_lanes = std::atoi(e);
     if (const char *e = std::getenv("SPAI_WS_BYTES"))
         prm.ws_bytes_per_warp = std::atoi(e);
+    if (const char *e = std::getenv("SPAI_QCAP"))
+        prm.first_qcap = std::atoi(e);
     prm.epsilon = opt->epsilon;
     // Every form follows the reference's sequential arithmetic bit for bit by default; the
     // group-parallel variant (parallel norms and mean, hashed candidate sets) is opt-in.
@@ -889,6 +915,34 @@ int spai_gmres(spai_handle *h, const double *rhs, double *x, double tau, int64_t
         *out_iterations = ctl.iterations;
     if (out_relative)
         *out_relative = ctl.rel;
+    return SPAI_OK;
+    API_END
+}
+
+int spai_history(spai_handle *h, spai_outer_record *outer, int64_t max_outer, int64_t *n_outer,
+                 spai_inner_record *inner, int64_t max_inner, int64_t *n_inner,
+                 spai_iteration_record *iterations, int64_t max_iterations, int64_t *n_iterations) {
+    API_BEGIN
+    if (!h || max_outer < 0 || max_inner < 0 || max_iterations < 0)
+        return fail(SPAI_ERR_ARGUMENT, "spai_history: bad arguments");
+    if (!h->hist_outer)
+        return fail(SPAI_ERR_NOT_BUILT, "spai_history: no solve with SPAI_FLAG_HISTORY on this handle");
+    SPAI_CUDA(cudaSetDevice(h->device));
+    SPAI_CUDA(cudaStreamSynchronize(h->stream));
+    auto copy = [&](auto *dst, const auto *src, int64_t maxc, int recorded, int cap) {
+        const int64_t cnt = std::min<int64_t>(maxc, std::min(recorded, cap));
+        if (dst && cnt > 0)
+            SPAI_CUDA(cudaMemcpy(dst, src, sizeof(*dst) * cnt, cudaMemcpyDeviceToHost));
+    };
+    copy(outer, h->hist_outer, max_outer, h->hist_n_outer, h->hist_cap_outer);
+    copy(inner, h->hist_inner, max_inner, h->hist_n_inner, h->hist_cap_inner);
+    copy(iterations, h->hist_iter, max_iterations, h->hist_n_iter, h->hist_cap_iter);
+    if (n_outer)
+        *n_outer = h->hist_n_outer;
+    if (n_inner)
+        *n_inner = h->hist_n_inner;
+    if (n_iterations)
+        *n_iterations = h->hist_n_iter;
     return SPAI_OK;
     API_END
 }

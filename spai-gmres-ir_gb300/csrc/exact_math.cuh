@@ -294,4 +294,5 @@ template <class T> SPAI_HD T cr_hypot(T a, T b) {
     return cr_hypot_general(x, y);
 }
 
+
 } // namespace spai

@@ -1,6 +1,7 @@
 // Device-side GMRES / iterative-refinement state shared by krylov.cu and the API layer.
 #pragma once
 #include "spai_internal.hpp"
+#include "spai_ir.h"
 
 namespace spai {
 
@@ -44,6 +45,14 @@ struct Ctl {
     double den, beta, est, hnext, rel, orig;
     int outer_cap;
     int counters[16];   // spare
+    // Refinement history (SPAI_FLAG_HISTORY): records written by the decision kernels; null
+    // pointers when not requested.
+    spai_outer_record *h_outer;
+    spai_inner_record *h_inner;
+    spai_iteration_record *h_iter;
+    int h_cap_outer, h_cap_inner, h_cap_iter;
+    int h_n_outer, h_n_inner, h_n_iter;
+    int h_iter_base;
 };
 
 struct GmresBuffers; // defined in krylov.cu
@@ -57,6 +66,7 @@ struct SolveSettings {
     bool scale_rhs = false; // mixed form: power-of-two scaled binary32 correction RHS
     bool accept_every = false; // binary32 drop-in acceptance (recomputed residual each step)
     bool use_graph = true;
+    bool history = false;      // record the refinement history (SPAI_FLAG_HISTORY)
 };
 
 } // namespace spai

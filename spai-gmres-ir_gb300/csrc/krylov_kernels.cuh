@@ -273,6 +273,14 @@ __global__ void decide_kernel(Ctl *ctl, const T *orig, const T *relnum) {
         const double rel = static_cast<double>(*relnum) / ctl->den;
         ctl->rel = rel;
         ctl->orig = static_cast<double>(*orig);
+        if (ctl->h_iter) {
+            const int idx = ctl->h_iter_base + ctl->k;
+            if (idx < ctl->h_cap_iter) {
+                ctl->h_iter[idx].recomputed_relative = rel;
+                ctl->h_iter[idx].accepted = isfinite(rel) && rel <= ctl->tol_inner &&
+                                            !(ctl->triggered == 2 && ctl->accept_every);
+            }
+        }
         if (!isfinite(rel) || !isfinite(ctl->orig)) {
             ctl->status = 8;
             ctl->active = 0;
@@ -334,6 +342,7 @@ template <class T> __global__ void gmres_start_kernel(Ctl *ctl, const T *orig, i
     ctl->formed = 0;
     ctl->active = 1;
     ctl->status = 7;
+    ctl->rel = NAN;
     const double r0 = static_cast<double>(*orig);
     ctl->orig = r0;
     if (!isfinite(r0)) {
@@ -378,7 +387,7 @@ __global__ void gmres_den_kernel(Ctl *ctl, const T *den, T *g, int accept_every)
 // Iterative refinement in TO (binary64 for F64/MIXED, binary32 for F32).
 // ------------------------------------------------------------------------------------------
 struct DiagPart {
-    double rinf, xinf, cbe;
+    double rinf, xinf, cbe, r2;
     int nonfinite;
 };
 
@@ -396,7 +405,7 @@ __global__ void __launch_bounds__(kBlock) ir_residual_kernel(int n, const int *_
     __shared__ double sh[32];
     const int lane = threadIdx.x & (G - 1);
     const int groups = (gridDim.x * blockDim.x) / G;
-    double rinf = 0, xinf = 0, cbe = 0;
+    double rinf = 0, xinf = 0, cbe = 0, r2 = 0;
     int bad = 0;
     const int warp_first = (blockIdx.x * blockDim.x + (threadIdx.x & ~31)) / G;
     const int sub = (threadIdx.x & 31) / G;
@@ -420,6 +429,7 @@ __global__ void __launch_bounds__(kBlock) ir_residual_kernel(int n, const int *_
             r[row] = res;
             bad |= !isfinite(res) || !isfinite(absacc);
             rinf = fmax(rinf, static_cast<double>(fabs(res)));
+            r2 += static_cast<double>(res) * static_cast<double>(res);
             xinf = fmax(xinf, static_cast<double>(fabs(x[row])));
             const double cden = static_cast<double>(fabs(b[row]) + absacc);
             const double ares = static_cast<double>(fabs(res));
@@ -437,19 +447,22 @@ __global__ void __launch_bounds__(kBlock) ir_residual_kernel(int n, const int *_
     xinf = block_reduce_max(xinf, sh);
     __syncthreads();
     cbe = block_reduce_max(cbe, sh);
+    __syncthreads();
+    r2 = ctl->h_outer ? block_reduce_sum(r2, sh) : 0.0;
     bad = __syncthreads_or(bad);
     if (threadIdx.x == 0)
-        part[blockIdx.x] = DiagPart{rinf, xinf, cbe, bad};
+        part[blockIdx.x] = DiagPart{rinf, xinf, cbe, r2, bad};
     if (!last_block(counter))
         return;
     if (threadIdx.x != 0)
         return;
-    double R = 0, X = 0, C = 0;
+    double R = 0, X = 0, C = 0, S2 = 0;
     int nonfinite = 0;
     for (int i = 0; i < static_cast<int>(gridDim.x); ++i) {
         R = fmax(R, part[i].rinf);
         X = fmax(X, part[i].xinf);
         C = fmax(C, part[i].cbe);
+        S2 += part[i].r2;
         nonfinite |= part[i].nonfinite;
     }
     ctl->rinf = R;
@@ -463,6 +476,12 @@ __global__ void __launch_bounds__(kBlock) ir_residual_kernel(int n, const int *_
     }
     const double be = den == TO(0) ? (R == 0 ? 0.0 : INFINITY) : static_cast<double>(static_cast<TO>(R) / den);
     ctl->be = be;
+    if (ctl->h_outer) { // IrResult::history entry of this iterate (src/ir.cpp:149-152, 177-183)
+        const int idx = ctl->outer_steps;
+        if (idx < ctl->h_cap_outer)
+            ctl->h_outer[idx] = spai_outer_record{idx, R, sqrt(S2), be, C};
+        ctl->h_n_outer = max(ctl->h_n_outer, idx + 1);
+    }
     if (be <= ctl->be_tol) {
         ctl->ir_status = 0;
         ctl->outer_active = 0;
@@ -530,6 +549,8 @@ template <class TO>
 __global__ void __launch_bounds__(kBlock) ir_commit_kernel(int n, TO *x, const TO *xn, const Ctl *ctl) {
     if (!ctl->pending || ctl->ir_status == 6)
         return;
+    if (blockIdx.x == 0 && threadIdx.x == 0 && ctl->h_inner && ctl->inner_attempts - 1 < ctl->h_cap_inner)
+        ctl->h_inner[ctl->inner_attempts - 1].update_applied = 1; // src/ir.cpp:184
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
         x[i] = xn[i];
 }
@@ -544,6 +565,13 @@ __global__ void ir_after_inner_kernel(Ctl *ctl) {
     ctl->inner_attempts += 1;
     ctl->inner_iterations_total += ctl->iterations;
     ctl->last_gmres_status = ctl->status;
+    if (ctl->h_inner) { // IrResult::inner_history entry (src/ir.cpp:158-164)
+        const int idx = ctl->inner_attempts - 1;
+        if (idx < ctl->h_cap_inner)
+            ctl->h_inner[idx] = spai_inner_record{ctl->status, 0, ctl->iterations, ctl->rel};
+        ctl->h_n_inner = max(ctl->h_n_inner, idx + 1);
+        ctl->h_iter_base += ctl->iterations;
+    }
     if (!ctl->converged) {
         ctl->ir_status = 3; // inner_failure
         ctl->outer_active = 0;
@@ -768,6 +796,30 @@ template <class T, class TO> struct IrEngine {
     // Right preconditioning (adjoint solves): the operator is (inner matrix)·P, GMRES starts from
     // rhs itself, the candidate is d = P·(V y) and its only check is the true residual.
     bool right = false;
+    // History buffers (SPAI_FLAG_HISTORY), in their own arena so enabling them never disturbs the
+    // solve workspace.
+    DeviceArena hist_mem;
+    spai_outer_record *hist_outer = nullptr;
+    spai_inner_record *hist_inner = nullptr;
+    spai_iteration_record *hist_iter = nullptr;
+    int hist_cap_outer = 0, hist_cap_inner = 0, hist_cap_iter = 0;
+    void arm_history(Ctl &h, const SolveSettings &s) {
+        if (!s.history)
+            return;
+        hist_mem.reset();
+        hist_cap_outer = s.outer_cap + 2;
+        hist_cap_inner = s.outer_cap + 1;
+        hist_cap_iter = static_cast<int>(std::min<long long>(static_cast<long long>(cap) * (s.outer_cap + 1), 1 << 20));
+        hist_outer = hist_mem.alloc<spai_outer_record>(hist_cap_outer);
+        hist_inner = hist_mem.alloc<spai_inner_record>(hist_cap_inner);
+        hist_iter = hist_mem.alloc<spai_iteration_record>(hist_cap_iter);
+        h.h_outer = hist_outer;
+        h.h_inner = hist_inner;
+        h.h_iter = hist_iter;
+        h.h_cap_outer = hist_cap_outer;
+        h.h_cap_inner = hist_cap_inner;
+        h.h_cap_iter = hist_cap_iter;
+    }
 
     // Kernel nodes executed by the last graph solve, from the device loop counters: 4 init
     // nodes; per GMRES solve 8 start nodes (7 with right preconditioning) and 6 update/residual
@@ -1152,6 +1204,7 @@ template <class T, class TO> struct IrEngine {
         h.inner_scale = 1.0;
         h.nrows = n;
         h.accept_every = s.accept_every ? 1 : 0;
+        arm_history(h, s);
         SPAI_CUDA(cudaMemcpyAsync(ctl, &h, sizeof(Ctl), cudaMemcpyHostToDevice, st));
         SPAI_CUDA(cudaMemsetAsync(counters, 0, 16 * sizeof(int), st));
         if (s.use_graph && !(prof && prof->on)) {

@@ -266,6 +266,31 @@ template <class T> struct ColumnArgs {
     unsigned long long *packed_top;
     unsigned long long packed_cap;
     int *error;        // bit0 packed output full, bit1 column exceeded the largest workspace
+    unsigned long long *phase; // optional cycle counters per fit phase (tuning aid), nullptr = off
+};
+
+// Cycle accounting of a fit by phase (lane 0's clock; only when ColumnArgs::phase is set).
+enum FitPhase : int { kPhShadow = 0, kPhQr, kPhResidual, kPhCandidates, kPhScores, kPhSelect, kPhCount };
+struct PhaseClock {
+    unsigned long long *out;
+    long long t = 0;
+    unsigned long long acc[kPhCount] = {0, 0, 0, 0, 0, 0};
+    __device__ explicit PhaseClock(unsigned long long *o) : out(o) {
+        if (out)
+            t = clock64();
+    }
+    __device__ void mark(int ph) {
+        if (out) {
+            const long long now = clock64();
+            acc[ph] += static_cast<unsigned long long>(now - t);
+            t = now;
+        }
+    }
+    __device__ void commit(int lane) {
+        if (out && lane == 0)
+            for (int i = 0; i < kPhCount; ++i)
+                atomicAdd(out + i, acc[i]);
+    }
 };
 
 // Columns one launch of the column kernel takes, and where its misfits go. Workspace tiers form a
@@ -493,6 +518,7 @@ __device__ int fit_column(const Grp &g, const ColumnArgs<T> &A, int k, char *ws,
     T last_res = T(NAN);
     int status = kNotAttempted;
     const T eps = A.eps;
+    PhaseClock clk(A.phase);
     for (;;) {
         bump.reset(0);
         // ---- shadow I: union of the row patterns of A over J ----
@@ -520,6 +546,7 @@ __device__ int fit_column(const Grp &g, const ColumnArgs<T> &A, int k, char *ws,
         grp_bitonic_sort(g, I, P1);
         const int m = grp_unique_except(g, I, L1, static_cast<const int *>(nullptr), 0);
         bump.reset(static_cast<size_t>(m) * 4);
+        clk.mark(kPhShadow);
         if (m < q) {
             status = kRankDeficient;
             break;
@@ -538,6 +565,7 @@ __device__ int fit_column(const Grp &g, const ColumnArgs<T> &A, int k, char *ws,
         g.sync();
         T pivot_ratio = 0;
         const int ls = grp_least_squares<FAST>(g, R, rhs, m, q, coef, v, pivot_ratio);
+        clk.mark(kPhQr);
         if (ls != kSuccess) {
             status = ls;
             break;
@@ -567,6 +595,7 @@ __device__ int fit_column(const Grp &g, const ColumnArgs<T> &A, int k, char *ws,
                     res = cr_hypot(res, s[i]);
             res = g.shfl(res, 0);
         }
+        clk.mark(kPhResidual);
         if (!isfinite(res)) {
             status = kNumericalFailure;
             break;
@@ -672,6 +701,7 @@ __device__ int fit_column(const Grp &g, const ColumnArgs<T> &A, int k, char *ws,
         grp_bitonic_sort(g, C, P2);
         c = grp_unique_except(g, C, L2, J, q);
         }
+        clk.mark(kPhCandidates);
         if (c == 0) {
             status = kEmptyCandidates;
             break;
@@ -733,6 +763,7 @@ __device__ int fit_column(const Grp &g, const ColumnArgs<T> &A, int k, char *ws,
             }
             mean = g.shfl(mean, 0);
         }
+        clk.mark(kPhScores);
         if (!isfinite(mean)) {
             status = kNumericalFailure;
             break;
@@ -798,7 +829,9 @@ __device__ int fit_column(const Grp &g, const ColumnArgs<T> &A, int k, char *ws,
         }
         q += nsel;
         g.sync();
+        clk.mark(kPhSelect);
     }
+    clk.commit(lane);
     // ---- publish the last completed fit (column.pattern/coefficients) ----
     long long off = 0;
     if (lane == 0) {
@@ -979,7 +1012,8 @@ struct TierPlan {
 // about 1,300 columns/s, the 1 MiB global tier about 2,900 columns/s on larger columns). Columns
 // that do not fit move up the chain and are fitted again from the start (fits are deterministic,
 // so the result does not depend on the tier that completes a column).
-inline std::vector<TierPlan> plan_tiers(size_t first_ws, int first_G, int max_threads, size_t smem_budget) {
+inline std::vector<TierPlan> plan_tiers(size_t first_ws, int first_G, int max_threads, size_t smem_budget,
+                                        int first_qcap) {
     std::vector<TierPlan> tiers;
     auto qcap_for = [](size_t ws) {
         return ws <= 4096 ? 32 : (ws <= 16384 ? 64 : (ws <= 65536 ? 256 : 1024));
@@ -993,7 +1027,7 @@ inline std::vector<TierPlan> plan_tiers(size_t first_ws, int first_G, int max_th
         groups = std::max(per_warp, (groups / per_warp) * per_warp);
         if (static_cast<size_t>(groups) * ws > smem_budget)
             break;
-        tiers.push_back(TierPlan{G, ws, groups, qcap_for(ws), false});
+        tiers.push_back(TierPlan{G, ws, groups, tiers.empty() && first_qcap > 0 ? first_qcap : qcap_for(ws), false});
         ws *= 2;
         if (ws > 16384)
             G = std::max(G, 16);
@@ -1065,7 +1099,7 @@ void SpaiBuilder<T>::construct(const DeviceCsr<T> &a, const SpaiParams &prm, cud
     // fewer, larger ones. Overrides come from SpaiParams.
     const bool heavy = a.max_row > 48 || static_cast<double>(nnz) > 12.0 * n;
     const int G0 = prm.group_lanes > 0 ? prm.group_lanes : (heavy ? 16 : 8);
-    const int ws_default = heavy ? 28672 : (sizeof(T) == 8 ? 12288 : 6144);
+    const int ws_default = heavy ? 28672 : (sizeof(T) == 8 ? 12288 : 5120);
     const size_t ws0 = prm.ws_bytes_per_warp > 0 ? prm.ws_bytes_per_warp : ws_default;
     const size_t smem_budget = 225 * 1024;
     // Threads per block within the register budget of one block (124 registers/thread for
@@ -1073,7 +1107,7 @@ void SpaiBuilder<T>::construct(const DeviceCsr<T> &a, const SpaiParams &prm, cud
     const int max_threads = sizeof(T) == 8 ? 512 : 768;
     if (ws0 > smem_budget)
         throw ArgumentError("SPAI workspace per group too large for one block's shared memory");
-    const std::vector<TierPlan> tiers = plan_tiers(ws0, G0, max_threads, smem_budget);
+    const std::vector<TierPlan> tiers = plan_tiers(ws0, G0, max_threads, smem_budget, prm.first_qcap);
     out.group_lanes = tiers[0].G;
     out.ws_bytes = static_cast<int>(tiers[0].ws);
     int sms = 0, dev = 0;
@@ -1090,9 +1124,14 @@ void SpaiBuilder<T>::construct(const DeviceCsr<T> &a, const SpaiParams &prm, cud
         SPAI_CUDA(cudaMemsetAsync(queue, 0, sizeof(int) * 64, st));
         SPAI_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
         SPAI_CUDA(cudaMemsetAsync(top, 0, sizeof(unsigned long long), st));
+        unsigned long long *phase = nullptr;
+        if (trace) {
+            phase = arena.alloc<unsigned long long>(kPhCount);
+            SPAI_CUDA(cudaMemsetAsync(phase, 0, sizeof(unsigned long long) * kPhCount, st));
+        }
         ColumnArgs<T> args{n, a.rp, a.ci, a.val, tp, ti, d, static_cast<T>(prm.epsilon), prm.alpha,
                            prm.beta, out.col_status, out.col_fits, out.col_growths, out.col_clamps,
-                           out.col_q, out.col_residual, off, pidx, pv, top, cap, err};
+                           out.col_q, out.col_residual, off, pidx, pv, top, cap, err, phase};
         out.overflow_columns = 0;
         out.overflow_columns_global = 0;
         int pending = n;          // columns the next tier takes
@@ -1131,6 +1170,18 @@ void SpaiBuilder<T>::construct(const DeviceCsr<T> &a, const SpaiParams &prm, cud
                 out.overflow_columns = h_next;
             pending = h_next;
             in_list = out_list;
+        }
+        if (trace && phase) {
+            unsigned long long hp[kPhCount];
+            SPAI_CUDA(cudaMemcpy(hp, phase, sizeof(hp), cudaMemcpyDeviceToHost));
+            double tot = 0;
+            for (unsigned long long v : hp)
+                tot += static_cast<double>(v);
+            static const char *names[kPhCount] = {"shadow", "qr", "residual", "candidates", "scores", "select"};
+            std::fprintf(stderr, "spai fit phases (lane-0 cycles, all tiers):");
+            for (int i = 0; i < kPhCount; ++i)
+                std::fprintf(stderr, " %s %.1f%%", names[i], tot > 0 ? 100.0 * hp[i] / tot : 0.0);
+            std::fprintf(stderr, "\n");
         }
         int h_err = 0;
         SPAI_CUDA(cudaMemcpyAsync(&h_err, err, sizeof(int), cudaMemcpyDeviceToHost, st));

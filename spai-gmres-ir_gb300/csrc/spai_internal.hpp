@@ -74,6 +74,7 @@ struct SpaiParams {
     int group_lanes = 0;         // lanes per column (4, 8, 16, 32); 0 = tuned default
     bool fast = false;           // parallel norms/mean, hashed candidates (not bit-reproducing)
     size_t overflow_ws_bytes = 0;
+    int first_qcap = 0;          // pattern capacity of the first workspace tier; 0 = by size
 };
 
 template <class T> struct SpaiOutput {

@@ -17,6 +17,7 @@ CLI_DIR = os.path.join(PKG, "_build")
 PRECISION = {"f64": 0, "f32": 1, "mixed": 2}
 FLAG_NO_GRAPH = 1
 FLAG_FAST_SPAI = 2
+FLAG_HISTORY = 4
 FLAG_EXACT_SPAI = 0  # sequential, bit-reproducing SPAI (the default)
 
 SPAI_STATUS = ["success", "not_attempted", "invalid_input", "rank_deficient", "numerical_failure",
@@ -51,6 +52,25 @@ class Options(ctypes.Structure):
                 ("tau", ctypes.c_double), ("innercap", ctypes.c_int64), ("outercap", ctypes.c_int64),
                 ("be_tolerance", ctypes.c_double), ("precision", ctypes.c_int32),
                 ("flags", ctypes.c_int32)]
+
+
+class OuterRecord(ctypes.Structure):
+    _fields_ = [("step", ctypes.c_int64), ("residual_inf", ctypes.c_double), ("residual_2", ctypes.c_double),
+                ("normwise_backward_error", ctypes.c_double), ("componentwise_backward_error", ctypes.c_double)]
+
+
+class InnerRecord(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int32), ("update_applied", ctypes.c_int32), ("iterations", ctypes.c_int64),
+                ("final_relative", ctypes.c_double)]
+
+
+class IterationRecord(ctypes.Structure):
+    _fields_ = [("inner", ctypes.c_int64), ("iteration", ctypes.c_int64), ("estimated_relative", ctypes.c_double),
+                ("recomputed_relative", ctypes.c_double), ("accepted", ctypes.c_int32), ("pad", ctypes.c_int32)]
+
+
+def _records(arr, count):
+    return [{f: getattr(arr[i], f) for f, _ in arr[i]._fields_ if f != "pad"} for i in range(count)]
 
 
 class Report(ctypes.Structure):
@@ -103,6 +123,7 @@ SIGNATURES = {
                                     ctypes.POINTER(Report)]),
     "spai_adjoint_device": (ctypes.c_int, [VP, ctypes.c_int64, VP, VP, VP, VP, ctypes.POINTER(Options),
                                            ctypes.POINTER(Report)]),
+    "spai_history": (ctypes.c_int, [VP, VP, ctypes.c_int64, I64P, VP, ctypes.c_int64, I64P, VP, ctypes.c_int64, I64P]),
     "spai_profile": (ctypes.c_int, [VP, ctypes.c_int32]),
     "spai_profile_read": (ctypes.c_int, [VP, ctypes.c_int32, F64P, I64P, F64P]),
     "spai_backward_error_noalloc": (ctypes.c_int, [VP, VP, VP, VP, VP]),
@@ -253,6 +274,18 @@ class Handle:
     def backward_error_noalloc(self, d_b, d_x, d_out, stream=None):
         """Allocation-free backward error of device vector x (see spai_backward_error_noalloc)."""
         _check(lib().spai_backward_error_noalloc(self._h, VP(d_b), VP(d_x), VP(d_out), stream))
+
+    def history(self):
+        """History of the last solve run with FLAG_HISTORY: (outer, inner, iterations) record lists."""
+        no, ni, nt = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        _check(lib().spai_history(self._h, None, 0, ctypes.byref(no), None, 0, ctypes.byref(ni), None, 0,
+                                  ctypes.byref(nt)))
+        outer = (OuterRecord * max(no.value, 1))()
+        inner = (InnerRecord * max(ni.value, 1))()
+        its = (IterationRecord * max(nt.value, 1))()
+        _check(lib().spai_history(self._h, outer, no.value, ctypes.byref(no), inner, ni.value, ctypes.byref(ni),
+                                  its, nt.value, ctypes.byref(nt)))
+        return _records(outer, no.value), _records(inner, ni.value), _records(its, nt.value)
 
     KERNEL_CLASSES = ("spmv_A", "spmv_P", "cgs_pass1", "cgs_pass2", "cgs_pass3")
 

@@ -25,7 +25,8 @@ UNITS = {
 }
 HEADERS = ["common.cuh", "exact_math.cuh", "spai_internal.hpp", "krylov.cuh", "krylov_kernels.cuh",
            "cgs_tiles.cuh", "adjoint.cuh", "mm_io.hpp"]
-CLIS = {"gpu_fp64_ir": "-DSOLVER_F64", "gpu_fp32_ir": "-DSOLVER_F32", "gpu_mixed_ir": "-DSOLVER_MIXED"}
+CLIS = {"gpu_fp64_ir": ("cli_main.cpp", "-DSOLVER_F64"), "gpu_fp32_ir": ("cli_main.cpp", "-DSOLVER_F32"),
+        "gpu_mixed_ir": ("cli_main.cpp", "-DSOLVER_MIXED"), "gpu_diag_ir": ("diag_main.cpp", "")}
 
 LIB = os.path.join(OUT, "libspai_ir.so")
 
@@ -58,12 +59,12 @@ def build(verbose=False, force=False):
         cmd = [NVCC] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart_static"]
         subprocess.run(cmd, check=True)
     cli_procs = []
-    for name, flag in CLIS.items():
+    for name, (src, flag) in CLIS.items():
         target = os.path.join(OUT, name)
-        deps = [os.path.join(CSRC, "cli_main.cpp"), LIB] + hdr
+        deps = [os.path.join(CSRC, src), LIB] + hdr
         if force or _stale(target, deps):
-            cmd = ["g++", "-O2", "-std=c++17", flag, "-I" + INCLUDE, "-I" + CSRC,
-                   os.path.join(CSRC, "cli_main.cpp"), "-o", target, "-L" + OUT, "-lspai_ir",
+            cmd = ["g++", "-O2", "-std=c++17"] + ([flag] if flag else []) + ["-I" + INCLUDE, "-I" + CSRC,
+                   os.path.join(CSRC, src), "-o", target, "-L" + OUT, "-lspai_ir",
                    "-Wl,-rpath,$ORIGIN"]
             cli_procs.append((cmd, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)))
     for cmd, p in cli_procs:

@@ -324,3 +324,54 @@ def test_device_hypot_matches_oracle(built, prec):
     want = np.array([ref(float(u), float(v)) for u, v in zip(a, b)])
     bad = np.flatnonzero(got != want)
     assert bad.size == 0, [(a[i], b[i], got[i], want[i]) for i in bad[:5]]
+
+
+# ---------------------------------------------------------------------------------------------
+# Refinement history (SPAI_FLAG_HISTORY) and the diagnostic CLI (src/cuda_hybrid_main.cpp)
+# ---------------------------------------------------------------------------------------------
+@pytest.mark.parametrize("prec", ["f64", "mixed"])
+def test_refinement_history(built, prec):
+    system = M.convection_diffusion_2d(32)
+    n = system[0]
+    opts = spai_ir.cli_options(n, prec, flags=spai_ir.FLAG_HISTORY)
+    with spai_ir.Handle(system, prec) as h:
+        h.build(opts)
+        x, rep = h.solve(M.equal_rhs(n), opts)
+        outer, inner, its = h.history()
+        _, rep_plain = h.solve(M.equal_rhs(n), spai_ir.cli_options(n, prec))
+    assert rep["converged"]
+    assert rep_plain["inner_iterations"] == rep["inner_iterations"]  # recording changes nothing
+    # IrResult::history: x0 then one record per applied correction
+    assert [o["step"] for o in outer] == list(range(rep["outer_steps"] + 1))
+    assert outer[-1]["normwise_backward_error"] == rep["backward_error"]
+    assert outer[-1]["componentwise_backward_error"] == rep["componentwise_backward_error"]
+    assert all(o["residual_2"] >= o["residual_inf"] for o in outer)
+    assert all(a["normwise_backward_error"] > b["normwise_backward_error"] for a, b in zip(outer, outer[1:]))
+    # inner_history / update_applied
+    assert len(inner) == rep["inner_attempts"]
+    assert sum(r["iterations"] for r in inner) == rep["inner_iterations"]
+    assert all(r["status"] == 0 and r["update_applied"] == 1 for r in inner)
+    # GmresResult::history: one record per Arnoldi step; the last of each solve is accepted
+    assert len(its) == rep["inner_iterations"]
+    for j, r in enumerate(inner, 1):
+        steps = [t for t in its if t["inner"] == j]
+        assert [t["iteration"] for t in steps] == list(range(1, r["iterations"] + 1))
+        assert steps[-1]["accepted"] == 1
+        assert steps[-1]["recomputed_relative"] == r["final_relative"]
+        assert np.isfinite([t["estimated_relative"] for t in steps]).all()
+        assert steps[-1]["estimated_relative"] <= (1e-8 if prec == "f64" else 1e-4)
+
+
+def test_diag_cli(built, tmp_path):
+    system = M.convection_diffusion_2d(24)
+    mtx = tmp_path / "c.mtx"
+    M.write_matrix_market(str(mtx), system)
+    out = subprocess.run([spai_ir.cli_path("gpu_diag_ir"), str(mtx)], capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0, out.stderr
+    steps = int(re.search(r"outer_steps=(\d+)", out.stdout).group(1))
+    attempts = int(re.search(r"inner_attempts=(\d+)", out.stdout).group(1))
+    assert len(re.findall(r"^outer=\d+ ", out.stdout, re.M)) == steps + 1
+    assert len(re.findall(r"^inner=\d+ status=success", out.stdout, re.M)) == attempts
+    assert len(re.findall(r"^inner_iteration=", out.stdout, re.M)) >= attempts
+    assert len(re.findall(r"^x\[\d+\]=", out.stdout, re.M)) == system[0]
+    assert "status=success converged=1" in out.stdout

@@ -65,7 +65,7 @@ def test_device_hypot_host_build_matches_oracle(built):
         assert spai_ir.hypotf(a, b) == O.hypotf(a, b)
 
 
-@pytest.mark.parametrize("cli", ["gpu_fp64_ir", "gpu_fp32_ir", "gpu_mixed_ir"])
+@pytest.mark.parametrize("cli", ["gpu_fp64_ir", "gpu_fp32_ir", "gpu_mixed_ir", "gpu_diag_ir"])
 def test_cli_input_errors(built, tmp_path, cli):
     exe = spai_ir.cli_path(cli)
     mtx = tmp_path / "tiny.mtx"
