@@ -73,7 +73,8 @@ enum {
     SPAI_ERR_WORKSPACE = -3, /* a SPAI column exceeded the largest fit workspace */
     SPAI_ERR_TIMEOUT = -4,   /* a bounded device wait gave up */
     SPAI_ERR_NOT_BUILT = -5, /* spai_solve before a successful spai_build */
-    SPAI_ERR_UNSUPPORTED = -6
+    SPAI_ERR_UNSUPPORTED = -6,
+    SPAI_ERR_FORMAT = -7     /* malformed input file (runtime_error of the reference's reader) */
 };
 
 /* Precision forms. F64 is the drop-in for gpu_fp64_ir; F32 for gpu_fp32_ir; MIXED builds the
@@ -235,6 +236,26 @@ int spai_adjoint(spai_handle *h, int64_t nrhs, const double *x, const double *dL
 int spai_adjoint_device(spai_handle *h, int64_t nrhs, const double *d_x, const double *d_dLdx,
                         double *d_dLdb, double *d_dLdA_values, const spai_options *opt,
                         spai_report *rep);
+
+/* Matrix Market reader on the device (read_matrix_market + CsrMatrix::from_entries,
+ * src/cpu.cpp:49-161): the host reads the file and its banner and size line; the GPU finds the
+ * lines, parses every entry, mirrors symmetric off-diagonals, stably sorts by (row, col), sums
+ * duplicates in input order and drops exact zeros. Accepted format, checks and results are the
+ * reference reader's: "%%MatrixMarket matrix coordinate real|integer general|symmetric",
+ * comment and blank lines skipped, one-based indices, finite values. Value tokens the device
+ * cannot convert with a certified correctly rounded result (more than 19 significant digits,
+ * hexadecimal or special tokens, results near a rounding midpoint, outside the normal range) are
+ * converted on the host by the C library's strtod, so the values are the same bits.
+ * Returns SPAI_ERR_FORMAT for malformed input, SPAI_ERR_ARGUMENT for invalid entries (the
+ * reference's invalid_argument), SPAI_ERR_CUDA for runtime failures. The CSR stays valid until
+ * spai_mm_free. No reference counterpart beyond the host reader it replaces. */
+typedef struct spai_mm_matrix_s spai_mm_matrix;
+/* device_min_lines: data sections with fewer lines are parsed on the host by the same rules
+ * (the transfer and launch overheads exceed the parse time; the CLIs pass 65536); 0 = always
+ * parse on the device. */
+int spai_mm_read(const char *path, int64_t device_min_lines, spai_mm_matrix **out);
+int spai_mm_csr(const spai_mm_matrix *m, spai_csr *csr, int64_t *cols, int64_t *host_converted_values);
+int spai_mm_free(spai_mm_matrix *m);
 
 /* History of the handle's last solve that ran with SPAI_FLAG_HISTORY: copies at most max_* records
  * of each kind and reports the recorded counts (n_* may exceed max_*; iteration records stop at

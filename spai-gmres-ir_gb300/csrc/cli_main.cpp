@@ -6,7 +6,7 @@
 //   exit 0 converged / 1 not converged or runtime error / 2 input error.
 // The solve runs on the device end to end (SPAI build, GMRES, refinement), so the banner says
 // cpu_outer=false where the reference printed cpu_outer=true.
-#include "mm_io.hpp"
+#include "cli_read.hpp"
 #include "spai_ir.h"
 
 #include <cmath>
@@ -54,10 +54,7 @@ int main(int argc, char **argv) {
         return 2;
     }
     try {
-        std::ifstream stream(argv[1]);
-        if (!stream)
-            throw std::invalid_argument("Cannot open Matrix Market input");
-        spai_io::HostCsr a = spai_io::read_matrix_market(stream);
+        spai_io::HostCsr a = spai_cli::read_matrix(argv[1]);
         if (!a.rows || a.rows != a.cols)
             throw std::invalid_argument("Solver requires a nonempty square matrix");
         const uint64_t n = a.rows;

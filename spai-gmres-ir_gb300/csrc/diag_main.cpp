@@ -7,7 +7,7 @@
 // (device-resident solve: no per-step host transfers) instead of the reference's transfer counters.
 // Recomputed relative residuals exist only for the steps where the acceptance rule verified a
 // candidate; the others print nan.
-#include "mm_io.hpp"
+#include "cli_read.hpp"
 #include "spai_ir.h"
 
 #include <cmath>
@@ -48,10 +48,7 @@ int main(int argc, char **argv) {
         return 2;
     }
     try {
-        std::ifstream input(argv[1]);
-        if (!input)
-            throw std::invalid_argument("Cannot open Matrix Market input");
-        spai_io::HostCsr a = spai_io::read_matrix_market(input);
+        spai_io::HostCsr a = spai_cli::read_matrix(argv[1]);
         if (!a.rows || a.rows != a.cols)
             throw std::invalid_argument("Hybrid IR requires a nonempty square matrix");
         const uint64_t n = a.rows;

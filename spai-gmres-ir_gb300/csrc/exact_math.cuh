@@ -295,4 +295,5 @@ template <class T> SPAI_HD T cr_hypot(T a, T b) {
 }
 
 
+
 } // namespace spai

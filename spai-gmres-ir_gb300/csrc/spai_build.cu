@@ -350,6 +350,17 @@ __device__ T grp_norm(const Grp &g, const T *x, int m, long long stride) {
 
 // Householder least squares with normalised reflectors, src/spai.cpp:30-98. R is destroyed,
 // rhs is transformed, coef receives the solution. Returns a SpaiStatus code.
+// The reference's left-to-right hypot chain over count elements (stride apart), one correctly
+// rounded hypot per step. (Speculative and software-pipelined variants of this chain, with the
+// exactness test moved off the dependency path, measured slower on the 128^3 system: 465-541 ms
+// against 388-401 ms for the whole SPAI.)
+template <class T> __device__ __forceinline__ T norm_chain(const T *x, int count, int stride) {
+    T r = 0;
+    for (int i = 0; i < count; ++i)
+        r = cr_hypot<T>(r, x[static_cast<long long>(i) * stride]);
+    return r;
+}
+
 template <bool FAST, class Grp, class T>
 __device__ int grp_least_squares(const Grp &g, T *R, T *rhs, int m, int q, T *coef, T *v,
                                  T &pivot_ratio) {
@@ -373,8 +384,7 @@ __device__ int grp_least_squares(const Grp &g, T *R, T *rhs, int m, int q, T *co
             length = grp_norm(g, R + static_cast<long long>(j) * q + j, m - j, q);
         } else {
             if (lane == 0)
-                for (int i = j; i < m; ++i)
-                    length = cr_hypot(length, R[static_cast<long long>(i) * q + j]);
+                length = norm_chain(R + static_cast<long long>(j) * q + j, m - j, q);
             length = g.shfl(length, 0);
         }
         if (!isfinite(length))
@@ -395,8 +405,7 @@ __device__ int grp_least_squares(const Grp &g, T *R, T *rhs, int m, int q, T *co
         } else {
             if (lane == 0) {
                 v[0] += copysign(T(1), v[0]);
-                for (int i = 0; i < m - j; ++i)
-                    vnorm = cr_hypot(vnorm, v[i]);
+                vnorm = norm_chain(v, m - j, 1);
             }
             vnorm = g.shfl(vnorm, 0);
         }
@@ -591,8 +600,7 @@ __device__ int fit_column(const Grp &g, const ColumnArgs<T> &A, int k, char *ws,
             res = grp_norm(g, s, m, 1);
         } else {
             if (lane == 0)
-                for (int i = 0; i < m; ++i)
-                    res = cr_hypot(res, s[i]);
+                res = norm_chain(s, m, 1);
             res = g.shfl(res, 0);
         }
         clk.mark(kPhResidual);

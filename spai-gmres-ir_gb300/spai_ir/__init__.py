@@ -32,6 +32,7 @@ IR_STATUS = ["success", "invalid_input", "construction_failure", "inner_failure"
  IR_NUMERICAL_FAILURE) = range(7)
 
 OK, ERR_ARGUMENT, ERR_CUDA, ERR_WORKSPACE, ERR_TIMEOUT, ERR_NOT_BUILT, ERR_UNSUPPORTED = 0, -1, -2, -3, -4, -5, -6
+ERR_FORMAT = -7
 
 
 class SpaiError(RuntimeError):
@@ -123,6 +124,9 @@ SIGNATURES = {
                                     ctypes.POINTER(Report)]),
     "spai_adjoint_device": (ctypes.c_int, [VP, ctypes.c_int64, VP, VP, VP, VP, ctypes.POINTER(Options),
                                            ctypes.POINTER(Report)]),
+    "spai_mm_read": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int64, ctypes.POINTER(VP)]),
+    "spai_mm_csr": (ctypes.c_int, [VP, ctypes.POINTER(Csr), I64P, I64P]),
+    "spai_mm_free": (ctypes.c_int, [VP]),
     "spai_history": (ctypes.c_int, [VP, VP, ctypes.c_int64, I64P, VP, ctypes.c_int64, I64P, VP, ctypes.c_int64, I64P]),
     "spai_profile": (ctypes.c_int, [VP, ctypes.c_int32]),
     "spai_profile_read": (ctypes.c_int, [VP, ctypes.c_int32, F64P, I64P, F64P]),
@@ -348,6 +352,24 @@ def score(rsq, dot, den, precision="f64"):
     out = np.zeros(3)
     _check(lib().spai_score(PRECISION[precision], rsq, dot, den, _p(out, F64P)))
     return int(out[0]), float(out[1]), bool(out[2])
+
+
+def mm_read(path, device_min_lines=0):
+    """Matrix Market file -> canonical CSR (n, ptr, idx, val) parsed on the device (spai_mm_read);
+    also returns the column count and how many value tokens the host converted."""
+    h = VP()
+    _check(lib().spai_mm_read(str(path).encode(), device_min_lines, ctypes.byref(h)))
+    try:
+        c = Csr()
+        cols, conv = ctypes.c_int64(), ctypes.c_int64()
+        _check(lib().spai_mm_csr(h, ctypes.byref(c), ctypes.byref(cols), ctypes.byref(conv)))
+        n, nnz = c.n, c.nnz
+        ptr = np.ctypeslib.as_array(c.row_offsets, (n + 1,)).copy()
+        idx = np.ctypeslib.as_array(c.col_indices, (nnz,)).copy() if nnz else np.zeros(0, np.int64)
+        val = np.ctypeslib.as_array(c.values, (nnz,)).copy() if nnz else np.zeros(0)
+        return (n, ptr, idx, val), cols.value, conv.value
+    finally:
+        lib().spai_mm_free(h)
 
 
 def hypot_device(a, b, precision="f64"):
