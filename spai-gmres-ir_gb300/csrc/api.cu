@@ -322,6 +322,7 @@ SolveSettings settings_for(const spai_handle *h, const spai_options &o, int cap)
     s.accept_every = h->precision == SPAI_PREC_F32;
     s.use_graph = (o.flags & SPAI_FLAG_NO_GRAPH) == 0;
     s.history = (o.flags & SPAI_FLAG_HISTORY) != 0;
+    s.restart_at_cap = (o.flags & SPAI_FLAG_RESTART_AT_CAP) != 0;
     return s;
 }
 

@@ -68,6 +68,7 @@ struct BatchArgs {
     const int *prp, *pci;
     const float *pv;
     int ga, gp; // lanes per row for A and P
+    int restart; // SPAI_FLAG_RESTART_AT_CAP
     const double *b;
     double *x, *r, *xn;
     float *w, *t, *rhs, *pb, *cand, *ax;
@@ -82,7 +83,7 @@ struct St {
     // GMRES
     int k, active, status, converged, triggered, breakdown, iterations, formed, vgate, reorth;
     int verifications, reorth_count;
-    double den, orig, wnorm, hnext;
+    double den, orig, wnorm, hnext, rel;
     // refinement
     int ir_status, outer_active, outer_steps, inner_attempts, inner_total, last_gmres, ir_started,
         changed, nonfinite;
@@ -392,6 +393,7 @@ __device__ void gmres(const BatchArgs &a, const BatchSys &d, St &s, const Smem &
     if (threadIdx.x == 0) {
         s.k = 0;
         s.triggered = s.breakdown = s.converged = s.iterations = s.formed = 0;
+        s.rel = NAN;
         s.active = 1;
         s.status = 7;
         s.orig = r0;
@@ -547,6 +549,7 @@ __device__ void gmres(const BatchArgs &a, const BatchSys &d, St &s, const Smem &
                     s.verifications += 1;
                     const double rel = static_cast<double>(relnum) / s.den;
                     s.orig = orig;
+                    s.rel = rel;
                     if (nf1 || nf2 || !isfinite(rel) || !isfinite(static_cast<double>(orig))) {
                         s.status = 8;
                         s.active = 0;
@@ -666,7 +669,10 @@ __global__ void __launch_bounds__(kBT, 2) batched_ir_kernel(BatchArgs a) {
                 s.inner_attempts += 1;
                 s.inner_total += s.iterations;
                 s.last_gmres = s.status;
-                if (!s.converged) {
+                // SPAI_FLAG_RESTART_AT_CAP: a cap-limited solve whose verified candidate reduced
+                // the preconditioned residual still supplies the correction.
+                const bool partial = a.restart && s.status == 6 && s.formed > 0 && s.rel < 1.0;
+                if (!s.converged && !partial) {
                     s.ir_status = 3; // inner_failure
                     s.outer_active = 0;
                 }
@@ -947,6 +953,7 @@ extern "C" int spai_ir_solve_batched(int64_t count, const spai_csr *systems, con
         a.outer_cap = static_cast<int>(opt->outercap);
         a.tau = tau;
         a.be_tol = spai_api::be_tol(*opt);
+        a.restart = (opt->flags & SPAI_FLAG_RESTART_AT_CAP) != 0 ? 1 : 0;
         a.order = dorder;
         a.queue = queue;
         a.sys = dsys;

@@ -31,6 +31,7 @@ struct Ctl {
     int ir_started;
     int nrows;        // n: GMRES cap < n -> iteration_limit, else nonconvergence
     int accept_every; // binary32 drop-in acceptance (verify every step)
+    int accept_partial; // SPAI_FLAG_RESTART_AT_CAP
     int vgate;        // verification kernels of this step run
     int pending;      // an update x_new = x + d awaits its diagnostics
     int guard;        // Arnoldi steps run in this solve (bounds every device-side loop)
@@ -67,6 +68,7 @@ struct SolveSettings {
     bool accept_every = false; // binary32 drop-in acceptance (recomputed residual each step)
     bool use_graph = true;
     bool history = false;      // record the refinement history (SPAI_FLAG_HISTORY)
+    bool restart_at_cap = false; // SPAI_FLAG_RESTART_AT_CAP
 };
 
 } // namespace spai

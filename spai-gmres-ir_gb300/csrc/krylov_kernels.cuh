@@ -572,7 +572,10 @@ __global__ void ir_after_inner_kernel(Ctl *ctl) {
         ctl->h_n_inner = max(ctl->h_n_inner, idx + 1);
         ctl->h_iter_base += ctl->iterations;
     }
-    if (!ctl->converged) {
+    // With SPAI_FLAG_RESTART_AT_CAP a cap-limited solve whose verified candidate reduced the
+    // preconditioned residual still supplies the correction (restart from the new residual).
+    const bool partial = ctl->accept_partial && ctl->status == 6 && ctl->formed > 0 && ctl->rel < 1.0;
+    if (!ctl->converged && !partial) {
         ctl->ir_status = 3; // inner_failure
         ctl->outer_active = 0;
     }
@@ -1204,6 +1207,7 @@ template <class T, class TO> struct IrEngine {
         h.inner_scale = 1.0;
         h.nrows = n;
         h.accept_every = s.accept_every ? 1 : 0;
+        h.accept_partial = s.restart_at_cap ? 1 : 0;
         arm_history(h, s);
         SPAI_CUDA(cudaMemcpyAsync(ctl, &h, sizeof(Ctl), cudaMemcpyHostToDevice, st));
         SPAI_CUDA(cudaMemsetAsync(counters, 0, 16 * sizeof(int), st));

@@ -124,3 +124,15 @@ def test_batched_workload_512_systems(built):
         if ro["converged"]:
             assert abs(ro["outer_steps"] - reps[i]["outer_steps"]) <= 1
             assert np.linalg.norm(xs[i] - xo, np.inf) <= 1e-9 * np.linalg.norm(xo, np.inf)
+
+
+def test_batched_workload_restart_at_cap(built):
+    """With SPAI_FLAG_RESTART_AT_CAP the cap-limited systems of the 512-system workload keep
+    refining (restarted GMRES(100) inside IR) and every system reaches the binary64 target."""
+    systems = M.batched_convection_diffusion(512, seed=0)
+    bs = [M.equal_rhs(s[0]) for s in systems]
+    opts = spai_ir.options("mixed", epsilon=0.3, alpha=5, innercap=100, flags=spai_ir.FLAG_RESTART_AT_CAP)
+    xs, reps = spai_ir.ir_solve_batched(systems, bs, opts)
+    bad = [(i, r["ir_status"], r["outer_steps"]) for i, r in enumerate(reps) if not r["converged"]]
+    assert not bad, bad
+    assert max(r["backward_error"] for r in reps) <= BE64

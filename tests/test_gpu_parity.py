@@ -375,3 +375,30 @@ def test_diag_cli(built, tmp_path):
     assert len(re.findall(r"^inner_iteration=", out.stdout, re.M)) >= attempts
     assert len(re.findall(r"^x\[\d+\]=", out.stdout, re.M)) == system[0]
     assert "status=success converged=1" in out.stdout
+
+
+# ---------------------------------------------------------------------------------------------
+# SPAI_FLAG_RESTART_AT_CAP: a cap-limited inner solve that reduced the residual supplies the
+# correction (restarted GMRES inside IR); without the flag the reference's inner_failure stands.
+# ---------------------------------------------------------------------------------------------
+@pytest.mark.parametrize("prec", ["f64", "mixed"])
+def test_restart_at_cap(built, prec):
+    system = M.convection_diffusion_2d(64)
+    n = system[0]
+    b = M.equal_rhs(n)
+    plain = spai_ir.options(prec, epsilon=0.3, alpha=5, innercap=8)
+    restart = spai_ir.options(prec, epsilon=0.3, alpha=5, innercap=8,
+                              flags=spai_ir.FLAG_RESTART_AT_CAP | spai_ir.FLAG_HISTORY)
+    with spai_ir.Handle(system, prec) as h:
+        h.build(plain)
+        _, r0 = h.solve(b, plain)
+        x, r1 = h.solve(b, restart)
+        outer, inner, _ = h.history()
+    assert r0["ir_status"] == spai_ir.IR_INNER_FAILURE and r0["gmres_status"] == 6
+    _, ro = O.ir(system, b, precision=prec, epsilon=0.3, alpha=5, innercap=8)
+    assert ro["status"] == spai_ir.IR_INNER_FAILURE  # the reference semantics
+    assert r1["converged"] and r1["backward_error"] <= 10 * 2.0 ** -53, r1
+    assert r1["outer_steps"] > 1
+    assert all(r["status"] in (0, 6) and r["update_applied"] == 1 for r in inner)
+    assert any(r["status"] == 6 for r in inner)
+    assert all(a["normwise_backward_error"] > c["normwise_backward_error"] for a, c in zip(outer, outer[1:]))
