@@ -34,7 +34,7 @@ double be_tol(const spai_options &o);
 namespace spai {
 inline namespace batched_detail {
 
-constexpr int kBT = 512;       // threads per CTA
+constexpr int kBT = 1024;      // threads per CTA (one CTA per SM)
 constexpr int kBW = kBT / 32;  // warps per CTA
 constexpr int kTR = 128;       // rows per basis tile (one float4 per lane)
 constexpr unsigned kFull = 0xffffffffu;
@@ -586,7 +586,7 @@ __device__ void gmres(const BatchArgs &a, const BatchSys &d, St &s, const Smem &
     }
 }
 
-__global__ void __launch_bounds__(kBT, 2) batched_ir_kernel(BatchArgs a) {
+__global__ void __launch_bounds__(kBT, 1) batched_ir_kernel(BatchArgs a) {
     extern __shared__ __align__(16) float dyn[];
     __shared__ St s;
     __shared__ double red[kBW];

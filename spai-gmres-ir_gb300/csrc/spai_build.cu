@@ -267,6 +267,7 @@ template <class T> struct ColumnArgs {
     unsigned long long packed_cap;
     int *error;        // bit0 packed output full, bit1 column exceeded the largest workspace
     unsigned long long *phase; // optional cycle counters per fit phase (tuning aid), nullptr = off
+    int dyn_scores;            // hand candidates out dynamically (heavy-tailed row lengths)
 };
 
 // Cycle accounting of a fit by phase (lane 0's clock; only when ColumnArgs::phase is set).
@@ -720,10 +721,14 @@ __device__ int fit_column(const Grp &g, const ColumnArgs<T> &A, int k, char *ws,
         int *sel = bump.take<int>(max(nsel_cap, 1));
         if (!sc || !sel)
             return kOverflow;
-        // ---- scores: one lane per candidate, ascending shadow order ----
+        // ---- scores: each candidate's dot/den by one lane in row (ascending shadow) order ----
+        // Short uniform rows (stencils): lanes take candidates round-robin. Heavy-tailed rows
+        // (dyn_scores): candidates are handed out dynamically, a lane that finishes a row taking
+        // the next unassigned one, so long rows do not leave the group's other lanes idle (rows
+        // are walked 16 entries per round). The arithmetic per candidate is the same either way.
         const T rsq = res * res;
         int first_fail = INT_MAX, my_status = kSuccess, my_clamps = 0;
-        for (int t = lane; t < c; t += GS) {
+        for (int t = lane; t < c && !A.dyn_scores; t += GS) {
             const int j = C[t];
             const int b = A.rp[j], e = A.rp[j + 1];
             const T dj = A.d[j];
@@ -747,6 +752,52 @@ __device__ int fit_column(const Grp &g, const ColumnArgs<T> &A, int k, char *ws,
             }
             if (st == kSuccess && clamped)
                 my_clamps += 1;
+        }
+        int next = 0; // first unassigned candidate (the same in every lane)
+        int t = -1, x = 0, xe = 0, j = 0;
+        T dj = 0, dot = 0, den = 0;
+        for (; A.dyn_scores;) {
+            const unsigned want = g.ballot(t < 0);
+            if (t < 0) {
+                const int cand = next + __popc(want & ((1u << lane) - 1u));
+                if (cand < c) {
+                    t = cand;
+                    j = C[t];
+                    x = A.rp[j];
+                    xe = A.rp[j + 1];
+                    dj = A.d[j];
+                    dot = 0;
+                    den = 0;
+                }
+            }
+            next += __popc(want);
+            if (!g.any(t >= 0))
+                break;
+            if (t < 0)
+                continue;
+            const int stop = min(xe, x + 16);
+            for (; x < stop; ++x) {
+                const int col = A.ci[x];
+                const int pos = lower_bound_int(I, m, col);
+                if (pos < m && I[pos] == col) {
+                    const T value = A.av[x] * dj;
+                    dot += s[pos] * value;
+                    den += value * value;
+                }
+            }
+            if (x < xe)
+                continue;
+            T score;
+            int clamped;
+            const int st = score_value<T>(rsq, dot, den, score, clamped);
+            sc[t] = score;
+            if (st != kSuccess && (FAST ? j : t) < first_fail) {
+                first_fail = FAST ? j : t;
+                my_status = st;
+            }
+            if (st == kSuccess && clamped)
+                my_clamps += 1;
+            t = -1;
         }
         const int ff = grp_min(g, first_fail);
         if (ff != INT_MAX) {
@@ -1040,7 +1091,7 @@ inline std::vector<TierPlan> plan_tiers(size_t first_ws, int first_G, int max_th
         if (ws > 16384)
             G = std::max(G, 16);
     }
-    tiers.push_back(TierPlan{32, size_t(1) << 20, 4, 4096, true});   // 1 MiB, 16 groups per SM
+    tiers.push_back(TierPlan{32, size_t(1) << 20, 4, 4096, true});   // 1 MiB, 24 groups per SM (register limit)
     tiers.push_back(TierPlan{32, size_t(32) << 20, 1, 65536, true}); // 32 MiB, at most 512 groups
     return tiers;
 }
@@ -1139,7 +1190,7 @@ void SpaiBuilder<T>::construct(const DeviceCsr<T> &a, const SpaiParams &prm, cud
         }
         ColumnArgs<T> args{n, a.rp, a.ci, a.val, tp, ti, d, static_cast<T>(prm.epsilon), prm.alpha,
                            prm.beta, out.col_status, out.col_fits, out.col_growths, out.col_clamps,
-                           out.col_q, out.col_residual, off, pidx, pv, top, cap, err, phase};
+                           out.col_q, out.col_residual, off, pidx, pv, top, cap, err, phase, heavy ? 1 : 0};
         out.overflow_columns = 0;
         out.overflow_columns_global = 0;
         int pending = n;          // columns the next tier takes
@@ -1156,7 +1207,7 @@ void SpaiBuilder<T>::construct(const DeviceCsr<T> &a, const SpaiParams &prm, cud
             char *gws = nullptr;
             long long blocks = (static_cast<long long>(pending) + tp_.groups_per_block - 1) / tp_.groups_per_block;
             if (tp_.global) {
-                const long long groups = std::min<long long>(pending, ti_ + 2 == tiers.size() ? sms * 16LL : 512LL);
+                const long long groups = std::min<long long>(pending, ti_ + 2 == tiers.size() ? sms * 24LL : 512LL);
                 blocks = (groups + tp_.groups_per_block - 1) / tp_.groups_per_block;
                 // one workspace for every launched group (blocks * groups_per_block >= groups)
                 gws = arena.alloc<char>(tp_.ws * static_cast<size_t>(blocks * tp_.groups_per_block));
