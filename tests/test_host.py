@@ -136,3 +136,68 @@ def test_bench_replica_max_over_ranks_gloo():
             p.join(120)
         assert all(p.exitcode == 0 for p in ps)
         assert out[0] == out[1] == 11.0
+
+
+def _py_read(text):
+    """Independent restatement of read_matrix_market + from_entries (src/cpu.cpp:49-161) for
+    valid inputs: one-based entries, symmetric mirrors, stable (row, col) order, duplicates summed
+    in input order, exact zero sums dropped."""
+    lines = [l for l in text.splitlines()[1:] if l.strip(" \t\r") and not l.strip(" \t\r").startswith("%")]
+    banner = text.splitlines()[0].split()
+    rows, cols, count = map(int, lines[0].split())
+    ent = []
+    for l in lines[1:1 + count]:
+        r, c, v = l.split()
+        r, c, v = int(r) - 1, int(c) - 1, float(v)
+        ent.append((r, c, v))
+        if banner[4] == "symmetric" and r != c:
+            ent.append((c, r, v))
+    ent.sort(key=lambda e: (e[0], e[1]))  # Python's sort is stable
+    ptr, idx, val = [0] * (rows + 1), [], []
+    i = 0
+    while i < len(ent):
+        r, c, s = ent[i]
+        i += 1
+        while i < len(ent) and ent[i][:2] == (r, c):
+            s += ent[i][2]
+            i += 1
+        if s != 0.0:
+            idx.append(c)
+            val.append(s)
+            ptr[r + 1] += 1
+    for r in range(rows):
+        ptr[r + 1] += ptr[r]
+    return rows, cols, np.array(ptr), np.array(idx), np.array(val)
+
+
+@pytest.mark.parametrize("sym", ["general", "symmetric"])
+def test_mm_reader_host_path_matches_restatement(built, tmp_path, sym):
+    rng = np.random.default_rng(3)
+    n = 40
+    lines = []
+    for k in range(600):
+        r, c = sorted(rng.integers(1, n + 1, 2), reverse=(sym == "symmetric"))
+        v = rng.choice(["%.17g" % rng.standard_normal(), "%d" % rng.integers(-3, 4), "1.5e-3", "-2."])
+        if k % 50 == 0:
+            lines.append("% comment")
+        lines.append("%d %d %s" % (r, c, v))
+    count = sum(1 for l in lines if not l.startswith("%"))
+    text = "%%MatrixMarket matrix coordinate real " + sym + "\n%d %d %d\n" % (n, n, count) + "\n".join(lines) + "\n"
+    p = tmp_path / "m.mtx"
+    p.write_text(text)
+    (nn, ptr, idx, val), cols, _ = spai_ir.mm_read(p, 1 << 62)  # host path: no GPU needed
+    rows, cols2, ptr2, idx2, val2 = _py_read(text)
+    assert nn == rows and cols == cols2
+    assert np.array_equal(ptr, ptr2) and np.array_equal(idx, idx2)
+    assert np.array_equal(val.view(np.uint64), val2.view(np.uint64))
+
+
+def test_mm_reader_host_path_errors(built, tmp_path):
+    p = tmp_path / "e.mtx"
+    p.write_text("%%MatrixMarket matrix coordinate real general\n3 3 2\n1 1 1\n4 1 2\n")
+    with pytest.raises(spai_ir.SpaiError) as e:
+        spai_ir.mm_read(p, 1 << 62)
+    assert e.value.code == spai_ir.ERR_FORMAT and "outside one-based" in str(e.value)
+    with pytest.raises(spai_ir.SpaiError) as e:
+        spai_ir.mm_read(tmp_path / "missing.mtx", 1 << 62)
+    assert e.value.code == spai_ir.ERR_ARGUMENT
