@@ -271,11 +271,13 @@ template <class T> struct ColumnArgs {
 };
 
 // Cycle accounting of a fit by phase (lane 0's clock; only when ColumnArgs::phase is set).
-enum FitPhase : int { kPhShadow = 0, kPhQr, kPhResidual, kPhCandidates, kPhScores, kPhSelect, kPhCount };
+enum FitPhase : int {
+    kPhShadow = 0, kPhQr, kPhResidual, kPhCandidates, kPhScores, kPhSelect, kPhQrNorms, kPhQrUpdate, kPhCount
+};
 struct PhaseClock {
     unsigned long long *out;
     long long t = 0;
-    unsigned long long acc[kPhCount] = {0, 0, 0, 0, 0, 0};
+    unsigned long long acc[kPhCount] = {0, 0, 0, 0, 0, 0, 0, 0};
     __device__ explicit PhaseClock(unsigned long long *o) : out(o) {
         if (out)
             t = clock64();
@@ -364,7 +366,7 @@ template <class T> __device__ __forceinline__ T norm_chain(const T *x, int count
 
 template <bool FAST, class Grp, class T>
 __device__ int grp_least_squares(const Grp &g, T *R, T *rhs, int m, int q, T *coef, T *v,
-                                 T &pivot_ratio) {
+                                 T &pivot_ratio, PhaseClock *clk = nullptr) {
     const int lane = g.thread_rank();
     constexpr int GS = Grp::size();
     if (m < q)
@@ -414,6 +416,8 @@ __device__ int grp_least_squares(const Grp &g, T *R, T *rhs, int m, int q, T *co
         for (int i = lane; i < m - j; i += GS)
             v[i] /= vnorm;
         g.sync();
+        if (clk)
+            clk->mark(kPhQrNorms);
         // Columns j..q-1 of R and the right-hand side (as column q) in parallel, one per lane.
         int bad = 0;
         for (int col = j + lane; col <= q; col += GS) {
@@ -438,6 +442,8 @@ __device__ int grp_least_squares(const Grp &g, T *R, T *rhs, int m, int q, T *co
         if (g.any(bad))
             return kNumericalFailure;
         g.sync();
+        if (clk)
+            clk->mark(kPhQrUpdate);
         if (lane == 0)
             R[static_cast<long long>(j) * q + j] = diagonal;
         g.sync();
@@ -574,7 +580,8 @@ __device__ int fit_column(const Grp &g, const ColumnArgs<T> &A, int k, char *ws,
             rhs[i] = I[i] == k ? T(1) : T(0);
         g.sync();
         T pivot_ratio = 0;
-        const int ls = grp_least_squares<FAST>(g, R, rhs, m, q, coef, v, pivot_ratio);
+        clk.mark(kPhQr); // gather
+        const int ls = grp_least_squares<FAST>(g, R, rhs, m, q, coef, v, pivot_ratio, &clk);
         clk.mark(kPhQr);
         if (ls != kSuccess) {
             status = ls;
@@ -1236,7 +1243,8 @@ void SpaiBuilder<T>::construct(const DeviceCsr<T> &a, const SpaiParams &prm, cud
             double tot = 0;
             for (unsigned long long v : hp)
                 tot += static_cast<double>(v);
-            static const char *names[kPhCount] = {"shadow", "qr", "residual", "candidates", "scores", "select"};
+            static const char *names[kPhCount] = {"shadow", "qr_other", "residual", "candidates",
+                                                  "scores", "select", "qr_norms", "qr_update"};
             std::fprintf(stderr, "spai fit phases (lane-0 cycles, all tiers):");
             for (int i = 0; i < kPhCount; ++i)
                 std::fprintf(stderr, " %s %.1f%%", names[i], tot > 0 ? 100.0 * hp[i] / tot : 0.0);
