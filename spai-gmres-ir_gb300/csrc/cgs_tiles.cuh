@@ -41,7 +41,7 @@ template <> struct TileGeom<float> {
 template <> struct TileGeom<double> {
     static constexpr int R = 64; // 512-byte segments
 };
-constexpr int kCgsThreads = 256;
+constexpr int kCgsThreads = 512;
 constexpr int kCgsJB = 192; // segments per shared-memory chunk (96 KiB)
 
 template <class T> struct Basis {
@@ -391,7 +391,7 @@ __global__ void __launch_bounds__(kCgsThreads) cgs_pass_kernel(CgsArgs<T> a) {
         // A warp owns the same segments (j = part mod P) for the whole launch: its per-lane dot
         // partials stay in registers across tiles (fixed order) and are reduced across lanes
         // once at the end. Shuffle-per-segment reduction is the fallback for longer sets.
-        constexpr int kOwn = 40;
+        constexpr int kOwn = 20;
         const bool reg_dots = (kk + P - 1) / P <= kOwn;
         T racc[kOwn];
 #pragma unroll
@@ -399,7 +399,7 @@ __global__ void __launch_bounds__(kCgsThreads) cgs_pass_kernel(CgsArgs<T> a) {
             racc[i] = 0;
         // Pass 2 keeps a warp's segments in registers between the update and the second dot
         // products when it owns few enough of them (one shared-memory read of the tile, not two).
-        constexpr int kCache = sizeof(T) == 4 ? 26 : 12;
+        constexpr int kCache = sizeof(T) == 4 ? 12 : 6;
         const bool cache = MODE == 2 && (kk + P - 1) / P <= kCache;
         V16 vr[kCache];
         auto update_part = [&](const T *tile) {

@@ -957,7 +957,7 @@ template <class T, class TO> struct IrEngine {
         ntiles = (n + R - 1) / R;
         // One block per SM: the pipeline stages take most of the shared memory (the static
         // arrays of the pass use about 10 KiB of the 227 KiB).
-        stage_segs = cgs_stage_segs<T>(cap, 216 * 1024);
+        stage_segs = cgs_stage_segs<T>(cap, 212 * 1024);
         cgs_dyn = cgs_dyn_smem<T>(cap, stage_segs);
         nblk_dots = std::min(ntiles, sms);
         ctl = arena.alloc<Ctl>(1);
