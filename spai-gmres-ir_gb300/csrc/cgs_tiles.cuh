@@ -333,12 +333,14 @@ __global__ void __launch_bounds__(kCgsThreads) cgs_pass_kernel(CgsArgs<T> a) {
     // for passes 1 and 2, W_{k+1} for pass 3), so no tile waits on a dependent global load.
     const int tseg = kk + 1;
     const bool streamed = tseg <= a.stage_segs;
+    // Partial updates of the warps (passes 2 and 3), shared by the streamed and chunked paths.
+    __shared__ __align__(16) typename Vec16<T>::V wpart_all[MODE >= 2 ? kCgsWarps : 1][32];
     if (streamed) {
         // ---- Streamed path: whole tiles through a ring of item slots in shared memory. ----
         using VT = Vec16<T>;
         using V16 = typename VT::V;
         constexpr int E = VT::E;
-        __shared__ __align__(16) V16 wpart[kCgsWarps][32];
+        auto &wpart = wpart_all;
         const int cs = a.stage_segs;
         for (int i = threadIdx.x; i < kCgsWarps * cs; i += blockDim.x)
             accw[i] = 0;
@@ -560,7 +562,138 @@ __global__ void __launch_bounds__(kCgsThreads) cgs_pass_kernel(CgsArgs<T> a) {
             ts = static_cast<T>(ldexp(dsq, -2 * te));
         }
     }
-    for (int t = blockIdx.x; !streamed && t < a.V.ntiles; t += gridDim.x) {
+    // ---- Chunked streaming (k + 2 > stage_segs): items are (tile, chunk) pairs of at most
+    // cs = stage_segs - 1 basis segments plus the source vector's segment. All warps share a
+    // chunk; warp w owns the segments j = w (mod warps) and adds its warp-reduced dots straight
+    // into acc[j] (one owner per j: no races, fixed order). Passes 2 and 3 accumulate their
+    // partial update over a tile's chunks in registers and combine the warps once, at the tile's
+    // last chunk; pass 2 then streams the tile's chunks again (L2-resident) for its second dots.
+    const bool chunked = !streamed && a.stage_segs >= 2;
+    if (chunked) {
+        using VT = Vec16<T>;
+        using V16 = typename VT::V;
+        constexpr int E = VT::E;
+        constexpr int kSegBytes = R * static_cast<int>(sizeof(T));
+        auto &wpart_c = wpart_all;
+        T *stage0 = region;
+        const int cs = a.stage_segs - 1;
+        const size_t stage_elems = static_cast<size_t>(a.stage_segs) * R;
+        const int nch = (kk + cs - 1) / cs;
+        const int per_tile = nch * (MODE == 2 ? 2 : 1);
+        const int my_tiles = a.V.ntiles > static_cast<int>(blockIdx.x)
+                                 ? (a.V.ntiles - 1 - static_cast<int>(blockIdx.x)) / static_cast<int>(gridDim.x) + 1
+                                 : 0;
+        const long long nitems = static_cast<long long>(my_tiles) * per_tile;
+        auto issue = [&](long long item) {
+            if (item < nitems) {
+                const int st = static_cast<int>(item % kCgsStages);
+                const int q = static_cast<int>(item / per_tile), rem = static_cast<int>(item % per_tile);
+                const int sweep = rem / nch, c = rem % nch;
+                const int t = static_cast<int>(blockIdx.x) + q * static_cast<int>(gridDim.x);
+                const int j0 = c * cs, j1 = min(kk, j0 + cs);
+                char *dst = reinterpret_cast<char *>(stage0 + st * stage_elems);
+                const char *src = reinterpret_cast<const char *>(a.V.seg(t, j0));
+                const int bytes = (j1 - j0) * kSegBytes;
+                for (int o = threadIdx.x * 16; o < bytes; o += kCgsThreads * 16)
+                    cp_async16(dst + o, src + o);
+                if (sweep == 0) { // the source segment goes after the chunk (slot cs)
+                    const char *ws = MODE == 3 ? reinterpret_cast<const char *>(a.V.seg(t, kk))
+                                               : reinterpret_cast<const char *>(a.w + static_cast<long long>(t) * R);
+                    for (int o = threadIdx.x * 16; o < kSegBytes; o += kCgsThreads * 16)
+                        cp_async16(dst + static_cast<size_t>(cs) * kSegBytes + o, ws + o);
+                }
+            }
+            asm volatile("cp.async.commit_group;\n" ::: "memory");
+        };
+        __syncthreads(); // coefficients and accumulators visible
+        for (int i = 0; i < kCgsStages; ++i)
+            issue(i);
+        V16 cur = VT::zero(), part4 = VT::zero();
+        double dsq = 0;
+        auto accumulate_norm = [&](V16 v) {
+            for (int e = 0; e < E; ++e) {
+                const T x = VT::get(v, e);
+                if (sizeof(T) == 4) {
+                    bad |= !isfinite(x);
+                    dsq += static_cast<double>(x) * static_cast<double>(x);
+                } else {
+                    ssq_add(x);
+                }
+            }
+        };
+        // Dots land in per-warp shared accumulators (slot j / warps of the owning warp) while k
+        // fits them; acc may be in global memory for long caps, where a read-modify-write per
+        // (tile, segment) would serialise on its latency.
+        const int cs_len = a.stage_segs;
+        const bool own_smem = kk <= kCgsWarps * cs_len;
+        T *myw = accw + warp * cs_len;
+        for (int i = threadIdx.x; i < kCgsWarps * cs_len; i += blockDim.x)
+            accw[i] = 0;
+        __syncthreads();
+        auto chunk_dots = [&](const T *sb, int j0, int j1) {
+            for (int j = j0 + ((warp - j0 % kCgsWarps) + kCgsWarps) % kCgsWarps; j < j1; j += kCgsWarps) {
+                T d = VT::dot(*reinterpret_cast<const V16 *>(sb + (j - j0) * R + lane * E), cur);
+                for (int o = 16; o > 0; o >>= 1)
+                    d += __shfl_xor_sync(0xffffffffu, d, o);
+                if (lane == 0) {
+                    if (own_smem)
+                        myw[j / kCgsWarps] += d;
+                    else
+                        acc[j] += d;
+                }
+            }
+        };
+        for (long long item = 0; item < nitems; ++item) {
+            const int st = static_cast<int>(item % kCgsStages);
+            asm volatile("cp.async.wait_group %0;\n" ::"n"(kCgsStages - 1) : "memory");
+            __syncthreads();
+            const T *sb = stage0 + st * stage_elems;
+            const int q = static_cast<int>(item / per_tile), rem = static_cast<int>(item % per_tile);
+            const int sweep = rem / nch, c = rem % nch;
+            const int t = static_cast<int>(blockIdx.x) + q * static_cast<int>(gridDim.x);
+            const int j0 = c * cs, j1 = min(kk, j0 + cs);
+            if (sweep == 0 && MODE == 1) {
+                if (c == 0) {
+                    cur = *reinterpret_cast<const V16 *>(sb + static_cast<size_t>(cs) * R + lane * E);
+                    if (warp == 0)
+                        accumulate_norm(cur);
+                }
+                chunk_dots(sb, j0, j1);
+            } else if (sweep == 0) {
+                if (c == 0)
+                    part4 = VT::zero();
+                for (int j = j0 + ((warp - j0 % kCgsWarps) + kCgsWarps) % kCgsWarps; j < j1; j += kCgsWarps)
+                    part4 = VT::axpy(cf[j], *reinterpret_cast<const V16 *>(sb + (j - j0) * R + lane * E), part4);
+                if (c == nch - 1) {
+                    wpart_c[warp][lane] = part4;
+                    __syncthreads();
+                    V16 tot = wpart_c[0][lane];
+                    for (int w2 = 1; w2 < kCgsWarps; ++w2)
+                        tot = VT::add(tot, wpart_c[w2][lane]);
+                    cur = VT::sub(*reinterpret_cast<const V16 *>(sb + static_cast<size_t>(cs) * R + lane * E), tot);
+                    if (warp == 0) {
+                        *reinterpret_cast<V16 *>(a.V.seg(t, kk) + lane * E) = cur; // W_{k+1}
+                        accumulate_norm(cur);
+                    }
+                }
+            } else {
+                chunk_dots(sb, j0, j1); // pass 2, second sweep: dots of w'
+            }
+            __syncthreads(); // the slot (and wpart_c) is free
+            issue(item + kCgsStages);
+        }
+        asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+        __syncthreads();
+        if (MODE <= 2 && own_smem) // one owner per j: a copy, not a sum
+            for (int j = threadIdx.x; j < kk; j += blockDim.x)
+                acc[j] = accw[(j % kCgsWarps) * cs_len + j / kCgsWarps];
+        if (sizeof(T) == 4 && dsq > 0) {
+            const int e2 = ilogb(dsq);
+            te = e2 >= 0 ? e2 / 2 : -((1 - e2) / 2);
+            ts = static_cast<T>(ldexp(dsq, -2 * te));
+        }
+    }
+    for (int t = blockIdx.x; !streamed && !chunked && t < a.V.ntiles; t += gridDim.x) {
         const int row0 = t * R;
         const int rows = min(R, a.n - row0);
         __syncthreads();

@@ -402,3 +402,24 @@ def test_restart_at_cap(built, prec):
     assert all(r["status"] in (0, 6) and r["update_applied"] == 1 for r in inner)
     assert any(r["status"] == 6 for r in inner)
     assert all(a["normwise_backward_error"] > c["normwise_backward_error"] for a, c in zip(outer, outer[1:]))
+
+
+# ---------------------------------------------------------------------------------------------
+# Long Arnoldi runs: steps whose tile exceeds a pipeline stage (k + 2 > about 180 segments) take
+# the chunked streaming path of the Gram-Schmidt passes; the results still follow the oracle.
+# ---------------------------------------------------------------------------------------------
+@pytest.mark.parametrize("prec,cap,tol", [("f64", 400, 1e-8), ("mixed", 300, 5e-3)])
+def test_long_gmres_chunked_passes(built, prec, cap, tol):
+    system = M.anisotropic_diffusion(64, seed=3)
+    n = system[0]
+    rhs = np.random.default_rng(7).standard_normal(n)
+    with spai_ir.Handle(system, prec) as h:
+        h.build(spai_ir.options(prec, epsilon=0.3, alpha=5))
+        p = h.preconditioner()
+        x, r = h.gmres(rhs, 1e-30, cap)
+        x2, r2 = h.gmres(rhs, 1e-30, cap)
+    assert r["iterations"] == cap and r["status"] == 6, r
+    np.testing.assert_array_equal(x, x2)  # deterministic
+    xo, ro = O.gmres(system, p, rhs, tol=1e-30, cap=cap, precision="f64" if prec == "f64" else "f32")
+    assert ro["iterations"] == cap
+    assert np.linalg.norm(x - xo) <= tol * np.linalg.norm(xo), np.linalg.norm(x - xo) / np.linalg.norm(xo)
