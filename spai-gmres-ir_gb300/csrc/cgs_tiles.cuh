@@ -630,17 +630,34 @@ __global__ void __launch_bounds__(kCgsThreads) cgs_pass_kernel(CgsArgs<T> a) {
         for (int i = threadIdx.x; i < kCgsWarps * cs_len; i += blockDim.x)
             accw[i] = 0;
         __syncthreads();
+        // A warp owns at most 16 segments of a chunk (cs <= 256): their 16 lane partials are
+        // reduced together by a reduce-scatter (16 shuffles and adds in all, not 5 per segment:
+        // the reductions dominated on the binary64 pipe), leaving lane u with owned segment u.
         auto chunk_dots = [&](const T *sb, int j0, int j1) {
-            for (int j = j0 + ((warp - j0 % kCgsWarps) + kCgsWarps) % kCgsWarps; j < j1; j += kCgsWarps) {
-                T d = VT::dot(*reinterpret_cast<const V16 *>(sb + (j - j0) * R + lane * E), cur);
-                for (int o = 16; o > 0; o >>= 1)
-                    d += __shfl_xor_sync(0xffffffffu, d, o);
-                if (lane == 0) {
-                    if (own_smem)
-                        myw[j / kCgsWarps] += d;
-                    else
-                        acc[j] += d;
+            const int jf = j0 + ((warp - j0 % kCgsWarps) + kCgsWarps) % kCgsWarps;
+            T p[16];
+#pragma unroll
+            for (int u = 0; u < 16; ++u) {
+                const int j = jf + u * kCgsWarps;
+                p[u] = j < j1 ? VT::dot(*reinterpret_cast<const V16 *>(sb + (j - j0) * R + lane * E), cur) : T(0);
+            }
+#pragma unroll
+            for (int m = 8; m >= 1; m >>= 1) {
+                const bool up = (lane & m) != 0;
+#pragma unroll
+                for (int i = 0; i < m; ++i) {
+                    const T send = up ? p[i] : p[i + m];
+                    const T keep = up ? p[i + m] : p[i];
+                    p[i] = keep + __shfl_xor_sync(0xffffffffu, send, m);
                 }
+            }
+            const T d = p[0] + __shfl_xor_sync(0xffffffffu, p[0], 16);
+            const int j = jf + (lane & 15) * kCgsWarps;
+            if (lane < 16 && j < j1) {
+                if (own_smem)
+                    myw[j / kCgsWarps] += d;
+                else
+                    acc[j] += d;
             }
         };
         for (long long item = 0; item < nitems; ++item) {
