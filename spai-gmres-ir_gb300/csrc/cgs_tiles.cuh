@@ -2,8 +2,7 @@
 //
 // Layout: the basis is stored in row tiles of R rows; tile t holds the R-row segments of all
 // cap+1 vectors contiguously (segment j of tile t at base + (t*(cap+1) + j)*R). A block that owns
-// tile t therefore streams one contiguous region of (k+1)*R*s bytes per pass, staged into shared
-// memory with cp.async in chunks of up to JB segments.
+// tile t therefore streams one contiguous region of (k+1)*R*s bytes per pass into shared memory.
 //
 // Vectors are stored unnormalised: v_j = s_j W_j with the scale s_j kept on the device, so the
 // Arnoldi step needs no normalisation pass (the next SpMV and every later pass apply s_j).
@@ -19,12 +18,12 @@
 // Streaming: while k + 1 segments fit in a pipeline stage, each block streams its tiles through
 // two shared-memory stages filled by asynchronous 16-byte copies (cp.async, one commit group per
 // stage): a tile's k + 1 segments are contiguous, several tiles share a stage when k is small,
-// and the next stage loads while the current one is consumed. Every warp owns
-// the segments j = warp (mod 8) of every tile: its dots are reduced across lanes into
-// accumulators it alone updates, the update combines the warps' partial sums in a fixed order,
+// and the next stage loads while the current one is consumed. Warps share a tile's segments
+// (warp p of the P sharing a tile takes j = p mod P): dots accumulate per lane in registers and
+// are reduced across lanes once, the update combines the warps' partial sums in a fixed order,
 // and pass 2 takes its second dot product from the resident stage (no re-read). The source
-// vector's segment travels in the same stage.
-// Larger k falls back to chunked cp.async staging.
+// vector's segment travels in the same stage. Larger k streams (tile, chunk) items through the
+// same stages (see the chunked path in the kernel).
 #pragma once
 #include "common.cuh"
 #include "exact_math.cuh"
@@ -42,7 +41,6 @@ template <> struct TileGeom<double> {
     static constexpr int R = 64; // 512-byte segments
 };
 constexpr int kCgsThreads = 512;
-constexpr int kCgsJB = 192; // segments per shared-memory chunk (96 KiB)
 
 template <class T> struct Basis {
     T *base;
@@ -90,7 +88,7 @@ template <class T> struct CgsArgs {
     Ctl *ctl;
     CgsScratch scr;
     int always_reorth;
-    int stage_segs;     // segments per pipeline stage (0: always chunked staging)
+    int stage_segs;     // segments per pipeline stage (at least 2)
     T *gacc;            // large caps: per-block dot accumulators and coefficients in global memory
     T *gcf;             //   ([gridDim][cap + 2] each); nullptr: both in shared memory
 };
@@ -99,7 +97,7 @@ constexpr int kCgsStages = 2;
 constexpr int kCgsWarps = kCgsThreads / 32;
 
 // Dynamic shared memory of a pass: accumulators, coefficients and per-warp accumulators first,
-// then the staging region (chunk buffer of the chunked path, or the stages of the streamed one).
+// then the staging region (kCgsStages stages of stage_segs segments).
 // Accumulators and coefficients ([cap + 2] each) live in shared memory up to this size, in
 // per-block global scratch beyond it (very long GMRES caps). Per-warp accumulators hold
 // stage_segs entries each (the streamed path runs only while k + 2 <= stage_segs).
@@ -122,10 +120,7 @@ template <class T> inline int cgs_stage_segs(int cap, size_t dyn_budget) {
     return static_cast<int>(std::min<size_t>(segs, static_cast<size_t>(cap) + 1));
 }
 template <class T> inline size_t cgs_dyn_smem(int cap, int stage_segs) {
-    constexpr int R = 512 / sizeof(T);
-    const size_t chunked = (static_cast<size_t>(kCgsJB) * R + R) * sizeof(T);
-    const size_t streamed = static_cast<size_t>(kCgsStages) * stage_segs * 512;
-    return cgs_region_offset<T>(cap, stage_segs) + std::max(chunked, streamed);
+    return cgs_region_offset<T>(cap, stage_segs) + static_cast<size_t>(kCgsStages) * stage_segs * 512;
 }
 
 // 16-byte vector of T per lane: a warp covers one 512-byte segment.
@@ -181,24 +176,6 @@ __device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
     const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
 }
-__device__ __forceinline__ void cp_async_wait_all() {
-    asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
-}
-
-// Load segments [j0, j1) of tile t into buf (rows of a partial last tile are copied too: the
-// basis storage is padded to whole tiles and kept zero beyond n).
-template <class T>
-__device__ __forceinline__ void load_chunk(const Basis<T> &V, int t, int j0, int j1, T *buf) {
-    constexpr int R = TileGeom<T>::R;
-    const char *src = reinterpret_cast<const char *>(V.seg(t, j0));
-    char *dst = reinterpret_cast<char *>(buf);
-    const int bytes = (j1 - j0) * R * static_cast<int>(sizeof(T));
-    for (int o = threadIdx.x * 16; o < bytes; o += blockDim.x * 16)
-        cp_async16(dst + o, src + o);
-    cp_async_wait_all();
-    __syncthreads();
-}
-
 template <class T> __device__ T block_sum(T v, T *red) {
     for (int o = 16; o > 0; o >>= 1)
         v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -297,11 +274,7 @@ __global__ void __launch_bounds__(kCgsThreads) cgs_pass_kernel(CgsArgs<T> a) {
     T *accw = gacc ? reinterpret_cast<T *>(dyn)
                    : cf + (ctl->cap + 2);                           // [warps][stage_segs] streamed path
     T *region = reinterpret_cast<T *>(dyn + cgs_region_offset<T>(ctl->cap, a.stage_segs)); // staging (128-byte aligned)
-    T *buf = region;                                                // chunked path: [kCgsJB * R]
-    T *wt = buf + kCgsJB * R;                                       // chunked path: [R]
-    constexpr int NP = kCgsThreads / R; // threads per row in the update
     __shared__ T red[kCgsThreads / 32];
-    __shared__ T part_sum[NP][R];
     const int k = ctl->k;
     const int kk = k + 1; // segments 0..k
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -709,70 +682,6 @@ __global__ void __launch_bounds__(kCgsThreads) cgs_pass_kernel(CgsArgs<T> a) {
             te = e2 >= 0 ? e2 / 2 : -((1 - e2) / 2);
             ts = static_cast<T>(ldexp(dsq, -2 * te));
         }
-    }
-    for (int t = blockIdx.x; !streamed && !chunked && t < a.V.ntiles; t += gridDim.x) {
-        const int row0 = t * R;
-        const int rows = min(R, a.n - row0);
-        __syncthreads();
-        // Current vector segment.
-        if (threadIdx.x < R) {
-            T v = 0;
-            if (threadIdx.x < rows)
-                v = MODE == 3 ? a.V.seg(t, kk)[threadIdx.x] : a.w[row0 + threadIdx.x];
-            wt[threadIdx.x] = v;
-        }
-        __syncthreads();
-        bool resident = false; // the single chunk [0, kk) is still in buf
-        if (MODE >= 2) {
-            // wt -= sum_j (h_j s_j) W_j over all chunks; NP threads per row split each chunk
-            // into contiguous sub-ranges, combined in fixed order.
-            const int row = threadIdx.x % R, part = threadIdx.x / R;
-            T accr = 0;
-            for (int j0 = 0; j0 < kk; j0 += kCgsJB) {
-                const int j1 = min(kk, j0 + kCgsJB);
-                load_chunk(a.V, t, j0, j1, buf);
-                const int len = j1 - j0, per = (len + NP - 1) / NP;
-                const int ja = j0 + min(len, part * per), jb = j0 + min(len, (part + 1) * per);
-#pragma unroll 4
-                for (int j = ja; j < jb; ++j)
-                    accr += cf[j] * buf[(j - j0) * R + row];
-                resident = (j0 == 0 && j1 == kk);
-                __syncthreads();
-            }
-            part_sum[part][row] = accr;
-            __syncthreads();
-            if (part == 0) {
-                T tot = 0;
-                for (int q = 0; q < NP; ++q)
-                    tot += part_sum[q][row];
-                const T nv = row < rows ? wt[row] - tot : T(0);
-                wt[row] = nv;
-                a.V.seg(t, kk)[row] = nv; // W_{k+1} (pad rows stay zero)
-            }
-            __syncthreads();
-        }
-        if (MODE <= 2) {
-            // d_j += W_j^T wt over this tile; one warp per basis vector.
-            for (int j0 = 0; j0 < kk; j0 += kCgsJB) {
-                const int j1 = min(kk, j0 + kCgsJB);
-                if (!resident)
-                    load_chunk(a.V, t, j0, j1, buf);
-                for (int j = j0 + warp; j < j1; j += nw) {
-                    const T *sg = buf + (j - j0) * R;
-                    T sdot = 0;
-#pragma unroll
-                    for (int i = lane; i < R; i += 32)
-                        sdot += sg[i] * wt[i];
-                    for (int o = 16; o > 0; o >>= 1)
-                        sdot += __shfl_xor_sync(0xffffffffu, sdot, o);
-                    if (lane == 0)
-                        acc[j] += sdot;
-                }
-                __syncthreads();
-            }
-        }
-        if (threadIdx.x < R)
-            ssq_add(wt[threadIdx.x]);
     }
     // Block combine of the per-thread (te, ts) pairs: common exponent, then a fixed-order sum.
     int be = te;

@@ -958,6 +958,8 @@ template <class T, class TO> struct IrEngine {
         // One block per SM: the pipeline stages take most of the shared memory (the static
         // arrays of the pass use about 10 KiB of the 227 KiB).
         stage_segs = cgs_stage_segs<T>(cap, 212 * 1024);
+        if (stage_segs < 2)
+            throw std::runtime_error("Gram-Schmidt staging does not fit in shared memory");
         cgs_dyn = cgs_dyn_smem<T>(cap, stage_segs);
         nblk_dots = std::min(ntiles, sms);
         ctl = arena.alloc<Ctl>(1);
