@@ -968,6 +968,15 @@ template <class T, class TO> struct IrEngine {
         sp = build_sell(arena, pp, sms, setup_st);
         SPAI_CUDA(cudaStreamSynchronize(setup_st));
         const size_t vcount = static_cast<size_t>(ntiles) * (cap + 1) * R;
+        {
+            size_t free_b = 0, total_b = 0;
+            SPAI_CUDA(cudaMemGetInfo(&free_b, &total_b));
+            if (vcount * sizeof(T) > free_b)
+                throw WorkspaceError("Krylov basis of " + std::to_string(cap + 1) + " vectors of " +
+                                     std::to_string(n) + " rows needs " +
+                                     std::to_string(vcount * sizeof(T) >> 20) + " MiB, more than the " +
+                                     std::to_string(free_b >> 20) + " MiB free on the device; lower innercap");
+        }
         V = arena.alloc<T>(vcount);
         SPAI_CUDA(cudaMemset(V, 0, vcount * sizeof(T))); // pad rows of the last tile stay zero
         sc = arena.alloc<T>(cap + 2);
