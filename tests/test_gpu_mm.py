@@ -148,3 +148,17 @@ def test_device_reader_integer_field_errors(built, tmp_path):
     _write(p, "%%MatrixMarket matrix coordinate integer general", "3 3 2", ["1 1 1", "2 2 1.5"])
     dev, host = _both(p)
     assert dev == host and dev[0] == spai_ir.ERR_FORMAT
+
+
+@pytest.mark.parametrize("text", [
+    "%%MatrixMarket matrix coordinate real general\r\n3 3 3\r\n1 1 2.5\r\n2 2 -1\r\n3 3 4e0\r\n",   # CRLF
+    "%%MatrixMarket matrix coordinate real general\n3 3 3\n1\t1\t2.5\n 2  2  -1 \n3 3 4e0",        # tabs, no final newline
+    "%%MatrixMarket matrix coordinate real general\n%c\n3 3 3\n\n1 1 2.5\n  \t \n2 2 -1\n%x\n3 3 4e0\n\n",  # blanks
+    "%%MatrixMarket matrix coordinate real general\n3 3 0\n",                                      # no entries
+    "%%MatrixMarket matrix coordinate real symmetric\n3 3 2\n2 1 0.1\n3 3 1E-300\n",                # small values
+])
+def test_device_reader_edge_spellings(built, tmp_path, text):
+    p = tmp_path / "x.mtx"
+    p.write_bytes(text.encode())
+    dev, host = _both(p)
+    _same(dev, host)
