@@ -205,13 +205,13 @@ __device__ double tile_pass(const float *__restrict__ w, float *__restrict__ V, 
                               : *reinterpret_cast<const float4 *>(w + t * kTR + lane * 4);
         if (MODE >= 2) {
             int j = 0;
-            for (; j + 4 <= kk; j += 4) {
-                float4 v[4];
+            for (; j + 8 <= kk; j += 8) { // eight segment loads in flight per lane
+                float4 v[8];
 #pragma unroll
-                for (int q = 0; q < 4; ++q)
+                for (int q = 0; q < 8; ++q)
                     v[q] = *reinterpret_cast<const float4 *>(tile + static_cast<long long>(j + q) * kTR);
 #pragma unroll
-                for (int q = 0; q < 4; ++q) {
+                for (int q = 0; q < 8; ++q) {
                     const float c = sm.cf[j + q];
                     wv.x -= c * v[q].x;
                     wv.y -= c * v[q].y;
