@@ -285,12 +285,15 @@ int spai_profile_read(spai_handle *h, int32_t cls, double *ms, int64_t *launches
  * handle's n; d_out: device array of 3 doubles receiving {normwise backward error,
  * componentwise backward error, ||b - A x||_inf}. The handle must hold A in binary64
  * (SPAI_PREC_F64 or SPAI_PREC_MIXED). Scratch (the residual and per-block partials) is a fixed
- * file-scope device array of 4 MiB + 33 KiB that every GPU loading the library keeps until exit;
+ * file-scope device array of 4 MiB + 33,024 bytes that every GPU loading the library keeps until exit;
  * systems with n > 524288 rows are rejected with SPAI_ERR_ARGUMENT. The first call on a device
  * looks up that array's address (once per device); make this first call before any stream
  * capture. All calls share the array and it keeps the last call's contents; calls that overlap
  * on the GPU race. stream: cudaStream_t to launch on, NULL = the handle's stream. The call is
- * asynchronous; synchronise the stream before reading d_out. */
+ * asynchronous; synchronise the stream before reading d_out. When x, b, A x or the norms are not
+ * finite, the call still returns SPAI_OK and d_out[0] (normwise) is NaN; d_out[1] and d_out[2]
+ * then hold whatever the non-finite values give (Inf or NaN). A caller treats a NaN in d_out[0]
+ * as the solve's numerical_failure. */
 int spai_backward_error_noalloc(spai_handle *h, const double *d_b, const double *d_x,
                                 double *d_out, void *stream);
 

@@ -25,7 +25,11 @@ namespace spai {
 constexpr int kNoallocBlock = 256;
 constexpr int kNoallocMaxBlocks = 1024;
 constexpr size_t kNoallocHeader = 256;                      // ticket counter
-constexpr size_t kNoallocPartials = kNoallocMaxBlocks * 32; // one record per block
+// Partial records (32 bytes each), split in two halves: records [0, 512) hold each block's
+// {||r||_inf, ||x||_inf, componentwise ratio, nonfinite flag}, records [512, 1024) the same
+// block's {||A||_inf, ||b||_inf}. That split is why a launch has at most kNoallocMaxBlocks / 2
+// blocks. Scratch total: 256 + 32,768 bytes of header and partials plus 4 MiB of residual.
+constexpr size_t kNoallocPartials = kNoallocMaxBlocks * 32;
 constexpr size_t kNoallocResidualBytes = size_t(4) << 20;  // 4 MiB of binary64 residual
 constexpr size_t kNoallocBytes = kNoallocHeader + kNoallocPartials + kNoallocResidualBytes;
 constexpr long long kNoallocMaxRows = static_cast<long long>(kNoallocResidualBytes / sizeof(double));

@@ -1,7 +1,7 @@
 """Regenerate tests/golden/*.npz from the reference's own CPU solvers.
 
 Needs the reference tree (only present where fixtures are regenerated, never on the GPU machine):
-    make -C oracle ref            # compiles golden_gen.cpp against the reference's src/*.cpp
+    make -C oracle ref REF=<reference tree>   # compiles golden_gen.cpp against its src/*.cpp
     python tests/golden/make_golden.py
 Each fixture stores the inputs' generator parameters plus the reference's outputs (statuses,
 patterns, exact binary64 values), so the oracle and the GPU path can be pinned to them.

@@ -45,6 +45,50 @@ def test_noalloc_backward_error_matches_solve_report(built):
             assert np.allclose(got, expected, rtol=REL, atol=0), (got, expected)
 
 
+@pytest.mark.parametrize("precision", ["mixed"])
+def test_noalloc_mixed_handle_on_a_caller_stream(built, precision):
+    """A mixed-precision handle (binary64 A kept beside the binary32 copy) and a call on a stream
+    the caller owns, compared with that solve's reported backward errors."""
+    import torch
+
+    system = M.convection_diffusion_2d(48)
+    n = system[0]
+    b = M.equal_rhs(n)
+    opts = spai_ir.cli_options(n, precision)
+    with spai_ir.Handle(system, precision) as h:
+        h.build(opts)
+        x, rep = h.solve(b, opts)
+        assert rep["converged"]
+        db = torch.from_numpy(b).cuda()
+        dx = torch.from_numpy(x).cuda()
+        out = torch.full((3,), float("nan"), dtype=torch.float64, device="cuda")
+        torch.cuda.synchronize()
+        side = torch.cuda.Stream()
+        expected = np.array([rep["backward_error"], rep["componentwise_backward_error"], rep["residual_inf"]])
+        for _ in range(2):
+            h.backward_error_noalloc(db.data_ptr(), dx.data_ptr(), out.data_ptr(), side.cuda_stream)
+            side.synchronize()
+            got = out.cpu().numpy()
+            assert np.allclose(got, expected, rtol=REL, atol=0), (got, expected)
+
+
+def test_noalloc_nonfinite_x_gives_nan(built):
+    """A non-finite x gives SPAI_OK with a NaN normwise backward error (the documented signal)."""
+    import torch
+
+    system = M.convection_diffusion_2d(16)
+    n = system[0]
+    with spai_ir.Handle(system, "f64") as h:
+        db = torch.from_numpy(M.equal_rhs(n)).cuda()
+        dx = torch.ones(n, dtype=torch.float64, device="cuda")
+        dx[5] = float("nan")
+        out = torch.zeros(3, dtype=torch.float64, device="cuda")
+        torch.cuda.synchronize()
+        h.backward_error_noalloc(db.data_ptr(), dx.data_ptr(), out.data_ptr())
+        torch.cuda.synchronize()
+        assert np.isnan(out.cpu().numpy()[0])
+
+
 def test_noalloc_rejects_systems_beyond_the_scratch_limit(built):
     import torch
 
