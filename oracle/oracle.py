@@ -44,13 +44,19 @@ def lib():
         L.oracle_spai_free.argtypes = [ctypes.c_void_p]
         L.oracle_gmres.argtypes = [ctypes.c_int, ctypes.c_int64, I64P, I64P, F64P, I64P, I64P, F64P,
                                    F64P, ctypes.c_double, ctypes.c_int64, ctypes.c_int, ctypes.c_int,
-                                   F64P, F64P]
+                                   ctypes.c_int, F64P, F64P]
         L.oracle_ir.restype = ctypes.c_int
         L.oracle_ir.argtypes = [ctypes.c_int, ctypes.c_int64, I64P, I64P, F64P, F64P, F64P, F64P, F64P, F64P]
         L.oracle_spai_sample.restype = ctypes.c_double
         L.oracle_spai_sample.argtypes = [ctypes.c_int, ctypes.c_int64, I64P, I64P, F64P, ctypes.c_double,
                                          ctypes.c_int64, ctypes.c_int64, I64P, ctypes.c_int64, ctypes.c_int,
                                          I64P]
+        L.oracle_spai_columns_sample.restype = ctypes.c_int64
+        L.oracle_spai_columns_sample.argtypes = [ctypes.c_int, ctypes.c_int64, I64P, I64P, F64P, ctypes.c_double,
+                                                 ctypes.c_int64, ctypes.c_int64, I64P, ctypes.c_int64,
+                                                 ctypes.c_int, I32P, I32P, I32P, I32P, F64P, I32P, I64P,
+                                                 I64P, F64P, ctypes.c_int64]
+        L.oracle_set_threads.argtypes = [ctypes.c_int]
         L.oracle_refine.restype = ctypes.c_int
         L.oracle_refine.argtypes = [ctypes.c_int64, I64P, I64P, F64P, I64P, I64P, F64P, F64P, F64P,
                                     F64P, F64P, F64P]
@@ -137,7 +143,8 @@ def score(rsq, dot, den, precision="f64"):
 
 
 IR_KEYS = ("status", "converged", "outer_steps", "inner_attempts", "inner_iterations", "nbe", "cbe",
-           "residual_inf", "forward", "spai_status", "nnz_p", "last_inner_status")
+           "residual_inf", "forward", "spai_status", "nnz_p", "last_inner_status", "spai_seconds",
+           "refine_seconds")
 
 
 def _ir_report(rep):
@@ -150,8 +157,9 @@ def _ir_report(rep):
 
 
 def ir(system, b, precision="f64", epsilon=0.3, alpha=None, beta=8, tau=None, innercap=0,
-       outercap=20, be_tolerance=0.0, reference=None, lazy=True):
-    """Full SPAI-GMRES-IR pipeline; returns (x, report dict)."""
+       outercap=20, be_tolerance=0.0, reference=None, lazy=True, wide=None):
+    """Full SPAI-GMRES-IR pipeline; returns (x, report dict). wide: binary32 GMRES dots and
+    norms accumulated in binary64 (None = by precision: on for mixed, off for f32)."""
     n, ptr, idx, val = _csr(system)
     if alpha is None:
         alpha = (n + 7) // 8
@@ -159,8 +167,9 @@ def ir(system, b, precision="f64", epsilon=0.3, alpha=None, beta=8, tau=None, in
         tau = 1e-8 if precision == "f64" else 1e-4
     b = np.ascontiguousarray(b, np.float64)
     x = np.zeros(n)
-    opts = np.array([epsilon, alpha, beta, tau, innercap, outercap, be_tolerance, 1 if lazy else 0], np.float64)
-    rep = np.zeros(12)
+    opts = np.array([epsilon, alpha, beta, tau, innercap, outercap, be_tolerance, 1 if lazy else 0,
+                     -1 if wide is None else int(bool(wide))], np.float64)
+    rep = np.zeros(14)
     ref = None if reference is None else np.ascontiguousarray(reference, np.float64)
     lib().oracle_ir(PRECISION[precision], n, _p(ptr, I64P), _p(idx, I64P), _p(val, F64P), _p(b, F64P),
                     None if ref is None else _p(ref, F64P), _p(opts, F64P), _p(x, F64P), _p(rep, F64P))
@@ -186,7 +195,7 @@ def refine(system, p_system, b, tau=1e-8, innercap=0, outercap=20, be_tolerance=
 GMRES_KEYS = ("status", "converged", "iterations", "final_original", "final_relative")
 
 
-def gmres(system, p_system, rhs, tol=1e-8, cap=0, precision="f64", accept_every=False, lazy=True):
+def gmres(system, p_system, rhs, tol=1e-8, cap=0, precision="f64", accept_every=False, lazy=True, wide=False):
     n, ptr, idx, val = _csr(system)
     _, pptr, pidx, pval = _csr(p_system)
     rhs = np.ascontiguousarray(rhs, np.float64)
@@ -194,7 +203,8 @@ def gmres(system, p_system, rhs, tol=1e-8, cap=0, precision="f64", accept_every=
     rep = np.zeros(5)
     lib().oracle_gmres(1 if precision == "f32" else 0, n, _p(ptr, I64P), _p(idx, I64P), _p(val, F64P),
                        _p(pptr, I64P), _p(pidx, I64P), _p(pval, F64P), _p(rhs, F64P), tol, cap,
-                       1 if accept_every else 0, 1 if lazy else 0, _p(x, F64P), _p(rep, F64P))
+                       1 if accept_every else 0, 1 if lazy else 0, 1 if wide else 0, _p(x, F64P),
+                       _p(rep, F64P))
     d = dict(zip(GMRES_KEYS, rep.tolist()))
     d["status"], d["converged"], d["iterations"] = int(d["status"]), bool(d["converged"]), int(d["iterations"])
     return x, d
@@ -209,6 +219,36 @@ def spai_sample_seconds(system, cols, epsilon=0.3, alpha=5, beta=8, precision="f
                                    _p(val, F64P), epsilon, alpha, beta, _p(cols, I64P), len(cols), threads,
                                    ctypes.byref(fits))
     return sec, fits.value
+
+
+def set_threads(threads):
+    """Threads for the SPAI construction's column fits (the result does not depend on it)."""
+    lib().oracle_set_threads(int(threads))
+
+
+def spai_columns(system, cols, epsilon=0.3, alpha=5, beta=8, precision="f64", threads=1):
+    """Adaptive fits of the listed columns only (no full construction): per-column status, fits,
+    growths, clamps, residual, assembly flag, and their rows of P (ptr over the list, idx, val)."""
+    n, ptr, idx, val = _csr(system)
+    cols = np.ascontiguousarray(cols, np.int64)
+    m = len(cols)
+    st, fi, gr, cl, bad = (np.zeros(m, np.int32) for _ in range(5))
+    res = np.zeros(m)
+    pp = np.zeros(m + 1, np.int64)
+    cap = max(64 * m, 1)
+    for _ in range(2):
+        pi = np.zeros(cap, np.int64)
+        pv = np.zeros(cap)
+        total = lib().oracle_spai_columns_sample(1 if precision in ("f32", "mixed") else 0, n, _p(ptr, I64P),
+                                                 _p(idx, I64P), _p(val, F64P), epsilon, alpha, beta,
+                                                 _p(cols, I64P), m, threads, _p(st, I32P), _p(fi, I32P),
+                                                 _p(gr, I32P), _p(cl, I32P), _p(res, F64P), _p(bad, I32P),
+                                                 _p(pp, I64P), _p(pi, I64P), _p(pv, F64P), cap)
+        if total <= cap:
+            return dict(status=st, fits=fi, growths=gr, clamps=cl, residual=res, assembly_bad=bad,
+                        p_ptr=pp, p_idx=pi[:total], p_val=pv[:total])
+        cap = int(total)
+    raise RuntimeError("oracle_spai_columns_sample: capacity")
 
 
 def hypot(a, b):

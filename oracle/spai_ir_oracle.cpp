@@ -411,6 +411,9 @@ template <class T> struct SpaiResult {
     Csr<T> p; // P = N^T D, canonical CSR (zeros dropped, src/cpu.cpp:49-78)
 };
 
+// Threads for the column fits of construct_spai (oracle_set_threads); 1 = sequential.
+static int g_threads = 1;
+
 // src/spai.cpp:314-374.
 template <class T>
 SpaiResult<T> construct_spai(const Csr<T> &a, const SpaiOptions &o, bool keep_history) {
@@ -458,8 +461,24 @@ SpaiResult<T> construct_spai(const Csr<T> &a, const SpaiOptions &o, bool keep_hi
     result.scaling = in.d;
     result.status = S_SUCCESS;
     result.columns.resize(n);
+    // Columns are independent (each fit reads only A, d and the column structure): they are
+    // fitted on g_threads threads in interleaved order; the overall status is then taken in
+    // column order, as the sequential loop of src/spai.cpp:329-336 does.
+    const int nthreads = static_cast<int>(std::max<int64_t>(1, std::min<int64_t>(g_threads, n / 256)));
+    if (nthreads > 1) {
+        std::vector<std::thread> pool;
+        for (int t = 0; t < nthreads; ++t)
+            pool.emplace_back([&, t] {
+                for (int64_t k = t; k < n; k += nthreads)
+                    result.columns[k] = construct_column(in, k, o, keep_history);
+            });
+        for (auto &th : pool)
+            th.join();
+    } else {
+        for (int64_t k = 0; k < n; ++k)
+            result.columns[k] = construct_column(in, k, o, keep_history);
+    }
     for (int64_t k = 0; k < n; ++k) {
-        result.columns[k] = construct_column(in, k, o, keep_history);
         if (result.columns[k].status != S_SUCCESS && result.status == S_SUCCESS) {
             result.status = result.columns[k].status;
             result.first_failed_column = k;
@@ -499,6 +518,12 @@ struct GmresOptions {
     int64_t max_iterations = 0; // 0 = n
     int accept_every_iteration = 0; // 1 = binary32 drop-in semantics (fp32_cuda_gmres.cu:409)
     int lazy_candidates = 1;        // form x0 + V y only when verification is triggered
+    // Binary32 dot products and 2-norms: 0 = sequential binary32 sums (the reference's CPU FP32
+    // solver, src/fp32_cpu.cpp:12-23); 1 = accumulated in binary64 and rounded once, a model of
+    // the reference's FP32 GPU solver, whose dots and norms are cuBLAS reductions
+    // (cublasSdot_64 / cublasSnrm2_64, src/fp32_cuda_gmres.cu:158-167) with tree-order error
+    // O(log n) ulps rather than the O(n) ulps of a sequential sum over n entries.
+    int wide_reductions = 0;
 };
 struct GmresReport {
     int status = G_INVALID_INPUT;
@@ -523,9 +548,30 @@ GmresReport gmres(const Csr<T> &a, const Csr<T> &p, const std::vector<T> &rhs,
             return rep;
     const int64_t cap = o.max_iterations == 0 ? n : o.max_iterations;
     solution.assign(n, 0);
+    const bool wide = o.wide_reductions && sizeof(T) == 4;
+    auto vnorm = [&](const std::vector<T> &v) -> T {
+        if (!wide)
+            return norm2_checked(v);
+        double s2 = 0;
+        for (T x : v)
+            s2 += static_cast<double>(x) * static_cast<double>(x);
+        return finite(static_cast<T>(std::sqrt(s2)));
+    };
+    auto vdot = [&](const std::vector<T> &a_, const std::vector<T> &b_) -> T {
+        T dot = 0;
+        if (!wide) {
+            for (int64_t i = 0; i < n; ++i)
+                dot = finite(dot + finite(a_[i] * b_[i]));
+            return dot;
+        }
+        double acc = 0;
+        for (int64_t i = 0; i < n; ++i)
+            acc += static_cast<double>(a_[i]) * static_cast<double>(b_[i]);
+        return finite(static_cast<T>(acc));
+    };
     try {
         // x0 = 0: A x0 = 0, original residual = rhs.
-        const T r0 = norm2_checked(rhs);
+        const T r0 = vnorm(rhs);
         rep.final_original = r0;
         if (r0 == 0) {
             const bool zero = std::all_of(rhs.begin(), rhs.end(), [](T v) { return v == 0; });
@@ -535,7 +581,7 @@ GmresReport gmres(const Csr<T> &a, const Csr<T> &p, const std::vector<T> &rhs,
             return rep;
         }
         const std::vector<T> pb = spmv(p, rhs);
-        const T den = norm2_checked(pb);
+        const T den = vnorm(pb);
         if (den == 0) {
             rep.status = G_ZERO_PRECONDITIONED_RHS;
             return rep;
@@ -559,11 +605,11 @@ GmresReport gmres(const Csr<T> &a, const Csr<T> &p, const std::vector<T> &rhs,
             std::vector<T> r(n);
             for (int64_t i = 0; i < n; ++i)
                 r[i] = finite(rhs[i] - ax[i]);
-            orig = norm2_checked(r);
+            orig = vnorm(r);
             const std::vector<T> pax = spmv(p, ax);
             for (int64_t i = 0; i < n; ++i)
                 r[i] = finite(pb[i] - pax[i]);
-            rel = finite(norm2_checked(r) / den);
+            rel = finite(vnorm(r) / den);
         };
         int64_t formed_count = 0;
         // Candidate x0 + V y from the first count Givens-rotated columns (gmres.cpp:47-65).
@@ -587,14 +633,12 @@ GmresReport gmres(const Csr<T> &a, const Csr<T> &p, const std::vector<T> &rhs,
             std::vector<T> w = spmv(p, spmv(a, basis[k]));
             std::vector<T> hcol(k + 2, 0);
             for (int64_t j = 0; j <= k; ++j) {
-                T dot = 0;
-                for (int64_t i = 0; i < n; ++i)
-                    dot = finite(dot + finite(basis[j][i] * w[i]));
+                const T dot = vdot(basis[j], w);
                 hcol[j] = dot;
                 for (int64_t i = 0; i < n; ++i)
                     w[i] = finite(w[i] - finite(dot * basis[j][i]));
             }
-            const T hnext = norm2_checked(w);
+            const T hnext = vnorm(w);
             hcol[k + 1] = hnext;
             const bool breakdown = hnext == 0;
             if (!breakdown) {
@@ -953,6 +997,82 @@ double spai_sample(const Csr<T> &a, const SpaiOptions &o, const int64_t *cols, i
     return sec;
 }
 
+// Sampled-column parity: the adaptive fits of the listed columns (construct_column, columns
+// split over nthreads threads) and their rows of P = N^T D as the full construction assembles
+// them (src/spai.cpp:351-373: value = m_jk d_j, exact zeros dropped). Per listed column i:
+// status/fits/growths/clamps/residual[i], P row in p_idx/p_val[p_ptr[i] .. p_ptr[i+1]).
+// Returns the total number of stored P entries; nothing is written to p_idx/p_val when that
+// exceeds cap (call again with room). assembly_bad[i] = 1 when the row's assembly leaves the
+// binary range (the full construction then reports numerical_failure).
+template <class T>
+int64_t spai_columns_sample(const Csr<T> &a, const SpaiOptions &o, const int64_t *cols, int64_t ncols,
+                            int nthreads, int32_t *status, int32_t *fits, int32_t *growths,
+                            int32_t *clamps, double *residual, int32_t *assembly_bad, int64_t *p_ptr,
+                            int64_t *p_idx, double *p_val, int64_t cap) {
+    SpaiInput<T> in;
+    in.a = &a;
+    const int64_t n = a.n;
+    in.d.resize(n);
+    for (int64_t r = 0; r < n; ++r) {
+        T mx = 0;
+        for (int64_t e = a.ptr[r]; e < a.ptr[r + 1]; ++e)
+            mx = std::max(mx, std::fabs(a.val[e]));
+        in.d[r] = T(1) / mx;
+    }
+    in.tptr.assign(n + 1, 0);
+    for (int64_t e = 0; e < a.nnz(); ++e)
+        ++in.tptr[a.idx[e] + 1];
+    for (int64_t i = 0; i < n; ++i)
+        in.tptr[i + 1] += in.tptr[i];
+    in.tidx.resize(a.nnz());
+    std::vector<int64_t> fill(in.tptr.begin(), in.tptr.end() - 1);
+    for (int64_t r = 0; r < n; ++r)
+        for (int64_t e = a.ptr[r]; e < a.ptr[r + 1]; ++e)
+            in.tidx[fill[a.idx[e]]++] = r;
+    if (nthreads < 1)
+        nthreads = 1;
+    std::vector<std::vector<int64_t>> rows_idx(ncols);
+    std::vector<std::vector<double>> rows_val(ncols);
+    std::vector<std::thread> pool;
+    for (int t = 0; t < nthreads; ++t)
+        pool.emplace_back([&, t] {
+            for (int64_t i = t; i < ncols; i += nthreads) {
+                const Column<T> c = construct_column(in, cols[i], o, false);
+                status[i] = c.status;
+                fits[i] = static_cast<int32_t>(c.fits);
+                growths[i] = static_cast<int32_t>(c.growths);
+                clamps[i] = static_cast<int32_t>(c.score_clamps);
+                residual[i] = static_cast<double>(c.residual);
+                assembly_bad[i] = 0;
+                for (size_t e = 0; e < c.pattern.size(); ++e) {
+                    const int64_t j = c.pattern[e];
+                    const T value = c.coefficients[e] * in.d[j];
+                    if (!std::isfinite(value) || (c.coefficients[e] != 0 && value == 0))
+                        assembly_bad[i] = 1;
+                    if (value != 0) {
+                        rows_idx[i].push_back(j);
+                        rows_val[i].push_back(static_cast<double>(value));
+                    }
+                }
+            }
+        });
+    for (auto &th : pool)
+        th.join();
+    int64_t total = 0;
+    p_ptr[0] = 0;
+    for (int64_t i = 0; i < ncols; ++i) {
+        total += static_cast<int64_t>(rows_idx[i].size());
+        p_ptr[i + 1] = total;
+    }
+    if (total > cap)
+        return total;
+    for (int64_t i = 0; i < ncols; ++i) {
+        std::copy(rows_idx[i].begin(), rows_idx[i].end(), p_idx + p_ptr[i]);
+        std::copy(rows_val[i].begin(), rows_val[i].end(), p_val + p_ptr[i]);
+    }
+    return total;
+}
+
 } // namespace orc
 
 // ------------------------------------------------------------------------------------------
@@ -967,6 +1087,11 @@ struct OracleSpai {
 };
 
 extern "C" {
+
+// Threads used by the SPAI construction's column fits (results do not depend on it).
+void oracle_set_threads(int threads) {
+    g_threads = threads < 1 ? 1 : threads;
+}
 
 double oracle_hypot(double a, double b) {
     return cr_hypot(a, b);
@@ -1117,8 +1242,9 @@ void oracle_spai_free(void *hp) {
 void oracle_gmres(int precision, int64_t n, const int64_t *aptr, const int64_t *aidx,
                   const double *aval, const int64_t *pptr, const int64_t *pidx, const double *pval,
                   const double *rhs, double tolerance, int64_t cap, int accept_every,
-                  int lazy, double *x_out, double *rep) {
+                  int lazy, int wide, double *x_out, double *rep) {
     GmresOptions o;
+    o.wide_reductions = wide;
     o.tolerance = tolerance;
     o.max_iterations = cap;
     o.accept_every_iteration = accept_every;
@@ -1145,9 +1271,12 @@ void oracle_gmres(int precision, int64_t n, const int64_t *aptr, const int64_t *
 
 // Full SPAI-GMRES-IR pipeline. precision: 0 = FP64 (cuda_gpu_spai_gmres_ir semantics),
 // 1 = FP32 (fp32_cuda_spai_gmres_ir semantics), 2 = mixed (FP32 SPAI/GMRES, FP64 IR).
-// opts = {epsilon, alpha, beta, tau, innercap, outercap, be_tolerance, lazy}
+// opts = {epsilon, alpha, beta, tau, innercap, outercap, be_tolerance, lazy, wide}; wide < 0 =
+// by precision (binary64-accumulated binary32 reductions for the mixed form, sequential binary32
+// sums for the FP32 form, whose goldens come from the reference's CPU FP32 solver).
 // rep  = {status, converged, outer_steps, inner_attempts, inner_iterations, nbe, cbe,
-//         residual_inf, forward, spai_status, nnz_p, last_inner_status}
+//         residual_inf, forward, spai_status, nnz_p, last_inner_status, spai_seconds,
+//         refine_seconds}
 int oracle_ir(int precision, int64_t n, const int64_t *ptr, const int64_t *idx, const double *val,
               const double *b, const double *reference, const double *opts, double *x_out,
               double *rep) {
@@ -1161,6 +1290,7 @@ int oracle_ir(int precision, int64_t n, const int64_t *ptr, const int64_t *idx, 
     o.be_tolerance = opts[6];
     o.gmres.lazy_candidates = static_cast<int>(opts[7]);
     o.gmres.accept_every_iteration = precision == 1;
+    o.gmres.wide_reductions = opts[8] < 0 ? (precision == 2 ? 1 : 0) : static_cast<int>(opts[8]);
     IrReport r;
     const Csr<double> a = make_csr(n, ptr, idx, val);
     bool finite_rhs = true;
@@ -1171,8 +1301,12 @@ int oracle_ir(int precision, int64_t n, const int64_t *ptr, const int64_t *idx, 
         rep[0] = I_INVALID_INPUT;
         return I_INVALID_INPUT;
     }
+    using clk = std::chrono::steady_clock;
+    const auto t_start = clk::now();
+    auto t_spai = t_start;
     if (precision == 0) {
         const auto s = construct_spai(a, o.spai, false);
+        t_spai = clk::now();
         r.spai_status = s.status;
         r.nnz_p = s.p.nnz();
         if (s.status != S_SUCCESS) {
@@ -1187,6 +1321,7 @@ int oracle_ir(int precision, int64_t n, const int64_t *ptr, const int64_t *idx, 
     } else {
         const Csr<float> af = to_float(a);
         const auto s = construct_spai(af, o.spai, false);
+        t_spai = clk::now();
         r.spai_status = s.status;
         r.nnz_p = s.p.nnz();
         if (s.status != S_SUCCESS) {
@@ -1218,6 +1353,8 @@ int oracle_ir(int precision, int64_t n, const int64_t *ptr, const int64_t *idx, 
     rep[9] = r.spai_status;
     rep[10] = static_cast<double>(r.nnz_p);
     rep[11] = r.last_inner_status;
+    rep[12] = std::chrono::duration<double>(t_spai - t_start).count();
+    rep[13] = std::chrono::duration<double>(clk::now() - t_spai).count();
     return r.status;
 }
 
@@ -1232,6 +1369,25 @@ double oracle_spai_sample(int precision, int64_t n, const int64_t *ptr, const in
     if (precision == 1)
         return spai_sample(to_float(a), o, cols, ncols, nthreads, fits_out);
     return spai_sample(a, o, cols, ncols, nthreads, fits_out);
+}
+
+// precision 0 = binary64 SPAI of A, 1 = binary32 SPAI of A rounded to binary32.
+int64_t oracle_spai_columns_sample(int precision, int64_t n, const int64_t *ptr, const int64_t *idx,
+                                   const double *val, double epsilon, int64_t alpha, int64_t beta,
+                                   const int64_t *cols, int64_t ncols, int nthreads, int32_t *status,
+                                   int32_t *fits, int32_t *growths, int32_t *clamps, double *residual,
+                                   int32_t *assembly_bad, int64_t *p_ptr, int64_t *p_idx, double *p_val,
+                                   int64_t cap) {
+    SpaiOptions o;
+    o.epsilon = epsilon;
+    o.alpha = alpha;
+    o.beta = beta;
+    const Csr<double> a = make_csr(n, ptr, idx, val);
+    if (precision == 1)
+        return spai_columns_sample(to_float(a), o, cols, ncols, nthreads, status, fits, growths, clamps,
+                                   residual, assembly_bad, p_ptr, p_idx, p_val, cap);
+    return spai_columns_sample(a, o, cols, ncols, nthreads, status, fits, growths, clamps, residual,
+                               assembly_bad, p_ptr, p_idx, p_val, cap);
 }
 
 // IR with a given preconditioner (refine_with_preconditioner, ir.cpp:138-204), binary64.

@@ -2,7 +2,7 @@
 // reference reader's exception classes: invalid_argument for invalid entries and unopenable
 // files (exit 2), runtime_error for malformed input (exit 1), as src/solver_main.cpp maps them.
 #pragma once
-#include "mm_io.hpp"
+#include "mm_text.hpp"
 #include "spai_ir.h"
 
 #include <memory>
@@ -10,7 +10,7 @@
 #include <string>
 
 namespace spai_cli {
-inline spai_io::HostCsr read_matrix(const char *path) {
+inline spai_mm::HostCsr read_matrix(const char *path) {
     spai_mm_matrix *raw = nullptr;
     const int rc = spai_mm_read(path, 65536, &raw);
     if (rc == SPAI_ERR_ARGUMENT)
@@ -21,7 +21,7 @@ inline spai_io::HostCsr read_matrix(const char *path) {
     spai_csr c;
     int64_t cols = 0;
     spai_mm_csr(m.get(), &c, &cols, nullptr);
-    spai_io::HostCsr a;
+    spai_mm::HostCsr a;
     a.rows = static_cast<uint64_t>(c.n);
     a.cols = static_cast<uint64_t>(cols);
     a.ptr.assign(c.row_offsets, c.row_offsets + c.n + 1);

@@ -48,7 +48,7 @@ int main(int argc, char **argv) {
         return 2;
     }
     try {
-        spai_io::HostCsr a = spai_cli::read_matrix(argv[1]);
+        spai_mm::HostCsr a = spai_cli::read_matrix(argv[1]);
         if (!a.rows || a.rows != a.cols)
             throw std::invalid_argument("Hybrid IR requires a nonempty square matrix");
         const uint64_t n = a.rows;

@@ -1,6 +1,8 @@
 // Matrix Market reader on the device (spai_mm_read): the reference's read_matrix_market and
 // CsrMatrix::from_entries (src/cpu.cpp:49-161) with the same accepted format, checks, error
-// precedence and results as the host reader in mm_io.hpp, which it replaces for large files.
+// precedence and results as the host reader in mm_text.hpp, which it replaces for large files.
+// Both readers apply the same per-line rules (mm_text.hpp: skipped lines, field splitting, index
+// tokens, the data-line checks): the kernel below calls them once per line.
 //
 // Host: read the file, parse the banner and the size line (a few bytes), upload the data section.
 // Device: newline positions (one select pass), one thread per line classifies it (blank, comment,
@@ -19,7 +21,7 @@
 // library's correctly rounded strtod with the host reader's checks. Either way the value is the
 // same bits as the host reader's.
 #include "common.cuh"
-#include "mm_io.hpp"
+#include "mm_text.hpp"
 #include "spai_internal.hpp"
 #include "spai_ir.h"
 
@@ -54,27 +56,13 @@ struct Pow10 {
     int e;
 };
 
-// Line statuses; negative values are errors, in the host reader's order of checks.
-enum LineStatus : int {
-    kData = 0,
-    kSkip = 1,
-    kMalformed = -1,   // "Malformed coordinate entry"
-    kExtra = -2,       // "Extra field in Matrix Market line"
-    kIndexToken = -3,  // "Expected a nonnegative integer dimension/index"
-    kIndexBig = -4,    // "Dimension/index exceeds size_t"
-    kIndexRange = -5,  // "Matrix Market index outside one-based dimensions"
-    kIntegerField = -6 // "Integer field requires integer value tokens"
-};
+// Line statuses: the shared per-line codes (negative values are errors in check order).
+using spai_mm::kLineData;
+using spai_mm::kLineSkip;
+using spai_mm::kLineIntegerField;
 
-const char *status_message(int s) {
-    switch (s) {
-    case kMalformed: return "Malformed coordinate entry";
-    case kExtra: return "Extra field in Matrix Market line";
-    case kIndexToken: return "Expected a nonnegative integer dimension/index";
-    case kIndexBig: return "Dimension/index exceeds size_t";
-    case kIndexRange: return "Matrix Market index outside one-based dimensions";
-    default: return "Integer field requires integer value tokens";
-    }
+inline const char *status_message(int s) {
+    return spai_mm::line_message(s);
 }
 
 // ---- double-double helpers (host table construction) ----
@@ -133,27 +121,6 @@ const std::vector<Pow10> &pow10_table() {
 }
 
 // ---- device parse ----
-__device__ __forceinline__ bool is_space(unsigned char c) {
-    return c == ' ' || c == '\t' || c == '\r' || c == '\v' || c == '\f' || c == '\n';
-}
-
-// Unsigned decimal index token (digits only), with the host reader's overflow rule.
-__device__ int parse_index(const unsigned char *s, int len, unsigned long long &v) {
-    v = 0;
-    if (len == 0)
-        return kIndexToken;
-    for (int i = 0; i < len; ++i)
-        if (s[i] < '0' || s[i] > '9')
-            return kIndexToken;
-    for (int i = 0; i < len; ++i) {
-        const unsigned long long d = s[i] - '0';
-        if (v > (ULLONG_MAX - d) / 10)
-            return kIndexBig;
-        v = v * 10 + d;
-    }
-    return kData;
-}
-
 // Decimal value token -> certified correctly rounded double, or false (host converts it).
 __device__ bool parse_value(const unsigned char *s, int len, const Pow10 *tab, double &out) {
     int i = 0;
@@ -264,46 +231,17 @@ __global__ void __launch_bounds__(256) mm_lines_kernel(MmArgs a) {
                                 ? a.nl[ln]
                                 : a.size;
         const unsigned char *s = a.buf + b;
-        const int len = static_cast<int>(e - b);
-        int st = kSkip, fb = 0;
+        const long long len = e - b;
+        int fb = 0;
         unsigned long long r = 0, c = 0;
         double v = 0;
-        int first = 0;
-        while (first < len && (s[first] == ' ' || s[first] == '\t' || s[first] == '\r'))
-            ++first;
-        if (first < len && s[first] != '%') {
-            // tokens
-            int tb[4], te[4], nt = 0, p = 0;
-            while (p < len && nt < 4) {
-                while (p < len && is_space(s[p]))
-                    ++p;
-                if (p >= len)
-                    break;
-                tb[nt] = p;
-                while (p < len && !is_space(s[p]))
-                    ++p;
-                te[nt++] = p;
-            }
-            if (nt < 3) {
-                st = kMalformed;
-            } else if (nt > 3) {
-                st = kExtra;
-            } else {
-                st = parse_index(s + tb[0], te[0] - tb[0], r);
-                if (st == kData)
-                    st = parse_index(s + tb[1], te[1] - tb[1], c);
-                if (st == kData && (r == 0 || c == 0 || r > a.rows || c > a.cols))
-                    st = kIndexRange;
-                if (st == kData) {
-                    if (!parse_value(s + tb[2], te[2] - tb[2], a.tab, v)) {
-                        fb = 1; // the host converts and checks this value token
-                    } else if (a.integer_field) {
-                        for (int q = tb[2]; q < te[2]; ++q)
-                            if (!(s[q] == '+' || s[q] == '-' || (s[q] >= '0' && s[q] <= '9')))
-                                st = kIntegerField;
-                    }
-                }
-            }
+        long long vb = 0, ve = 0;
+        int st = spai_mm::classify_data_line(s, len, a.rows, a.cols, r, c, vb, ve);
+        if (st == kLineData) {
+            if (!parse_value(s + vb, static_cast<int>(ve - vb), a.tab, v))
+                fb = 1; // the host converts and checks this value token
+            else if (a.integer_field && !spai_mm::integer_token(s + vb, ve - vb))
+                st = kLineIntegerField;
         }
         a.status[ln] = st;
         a.fallback[ln] = fb;
@@ -327,7 +265,7 @@ __global__ void mm_place_kernel(long long nlines, long long count, const int *st
                                 unsigned long long cols, unsigned long long *keys, double *vals) {
     for (long long ln = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; ln < nlines;
          ln += static_cast<long long>(gridDim.x) * blockDim.x) {
-        if (status[ln] != kData)
+        if (status[ln] != kLineData)
             continue;
         const long long d = dataidx[ln];
         if (d >= count)
@@ -347,9 +285,9 @@ __global__ void mm_flags_kernel(long long nlines, const int *status, const unsig
                                 const unsigned long long *col, int symmetric, long long *isdata, long long *ismir) {
     for (long long ln = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; ln < nlines;
          ln += static_cast<long long>(gridDim.x) * blockDim.x) {
-        const bool data = status[ln] != kSkip;
+        const bool data = status[ln] != kLineSkip;
         isdata[ln] = data ? 1 : 0;
-        ismir[ln] = data && status[ln] == kData && symmetric && row[ln] != col[ln] ? 1 : 0;
+        ismir[ln] = data && status[ln] == kLineData && symmetric && row[ln] != col[ln] ? 1 : 0;
     }
 }
 
@@ -359,7 +297,7 @@ __global__ void mm_scan_errors_kernel(long long nlines, long long count, const i
                                       long long *fb_lines, unsigned long long *fb_count) {
     for (long long ln = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; ln < nlines;
          ln += static_cast<long long>(gridDim.x) * blockDim.x) {
-        if (status[ln] == kSkip || dataidx[ln] >= count)
+        if (status[ln] == kLineSkip || dataidx[ln] >= count)
             continue;
         if (status[ln] < 0)
             atomicMin(first_err, static_cast<unsigned long long>(ln));
@@ -410,26 +348,6 @@ __global__ void mm_compact_kernel(long long ne, const unsigned long long *keys, 
     }
 }
 
-struct FormatError : std::runtime_error {
-    using std::runtime_error::runtime_error;
-};
-
-// Host parse of one value token with the host reader's checks (src/cpu.cpp value handling).
-double host_value(const std::string &vt, bool integer_field) {
-    size_t used = 0;
-    double v;
-    try {
-        v = std::stod(vt, &used);
-    } catch (const std::exception &) {
-        throw FormatError("Invalid coordinate value");
-    }
-    if (used != vt.size() || !std::isfinite(v))
-        throw FormatError("Coordinate value must be finite and numeric");
-    if (integer_field && vt.find_first_not_of("+-0123456789") != std::string::npos)
-        throw FormatError("Integer field requires integer value tokens");
-    return v;
-}
-
 } // namespace mm_detail
 } // namespace spai
 
@@ -471,64 +389,17 @@ extern "C" int spai_mm_read(const char *path, int64_t device_min_lines, spai_mm_
         unsigned char *hbuf = hstore.data(); // pageable: the host path needs no GPU at all
         if (fsize > 0 && std::fread(hbuf, 1, static_cast<size_t>(fsize), f) != static_cast<size_t>(fsize))
             return mm_fail(SPAI_ERR_FORMAT, "Cannot read Matrix Market input");
-        long long pos = 0;
-        auto next_line = [&](std::string &line) {
-            if (pos >= fsize)
-                return false;
-            const unsigned char *e = static_cast<const unsigned char *>(std::memchr(hbuf + pos, '\n', fsize - pos));
-            const long long end = e ? e - hbuf : fsize;
-            line.assign(reinterpret_cast<const char *>(hbuf + pos), static_cast<size_t>(end - pos));
-            pos = e ? end + 1 : fsize;
-            return true;
-        };
-        std::string text;
-        if (!next_line(text))
-            return mm_fail(SPAI_ERR_FORMAT, "Missing Matrix Market banner");
-        std::string magic, object, format, field, symmetry;
-        {
-            std::istringstream banner(text);
-            if (!(banner >> magic >> object >> format >> field >> symmetry))
-                return mm_fail(SPAI_ERR_FORMAT, "Malformed Matrix Market banner");
-            std::string extra;
-            if (banner >> extra)
-                return mm_fail(SPAI_ERR_FORMAT, "Extra field in Matrix Market line");
-        }
-        if (magic != "%%MatrixMarket" || object != "matrix" || format != "coordinate" ||
-            (field != "real" && field != "integer") || (symmetry != "general" && symmetry != "symmetric"))
-            return mm_fail(SPAI_ERR_FORMAT, "Unsupported Matrix Market format");
-        bool found = false;
-        while (next_line(text)) {
-            const size_t b = text.find_first_not_of(" \t\r");
-            if (b != std::string::npos && text[b] != '%') {
-                found = true;
-                break;
-            }
-        }
-        if (!found)
-            return mm_fail(SPAI_ERR_FORMAT, "Missing matrix dimensions");
-        std::string rt, ct, nt;
-        std::istringstream dims(text);
-        if (!(dims >> rt >> ct >> nt))
-            return mm_fail(SPAI_ERR_FORMAT, "Malformed matrix dimensions");
-        {
-            std::string extra;
-            if (dims >> extra)
-                return mm_fail(SPAI_ERR_FORMAT, "Extra field in Matrix Market line");
-        }
-        const uint64_t rows = spai_io::detail::parse_size(rt), cols = spai_io::detail::parse_size(ct),
-                       count = spai_io::detail::parse_size(nt);
-        if (rows == 0 || cols == 0)
-            return mm_fail(SPAI_ERR_FORMAT, "Matrix dimensions must be positive");
-        const bool symmetric = symmetry == "symmetric", integer_field = field == "integer";
-        if (symmetric && rows != cols)
-            return mm_fail(SPAI_ERR_FORMAT, "Symmetric matrix must be square");
+        spai_mm::LineCursor cursor(reinterpret_cast<const char *>(hbuf), static_cast<size_t>(std::max<long long>(fsize, 0)));
+        const spai_mm::Header hdr = spai_mm::read_header(cursor); // runtime_error -> SPAI_ERR_FORMAT
+        const long long pos = static_cast<long long>(cursor.position());
+        const uint64_t rows = hdr.rows, cols = hdr.cols, count = hdr.count;
+        const bool symmetric = hdr.symmetric, integer_field = hdr.integer_field;
         const long long dsize = fsize - pos; // data section
         const long long approx_lines = dsize / 8 + 1;
         if (approx_lines < device_min_lines || dsize > INT_MAX - 1 || rows >= (1ull << 31) || cols >= (1ull << 31) ||
             count >= (1ull << 31)) {
             // host parse by the same rules (small files; or beyond the device path's 32-bit sizes)
-            std::istringstream in(std::string(reinterpret_cast<const char *>(hbuf), static_cast<size_t>(fsize)));
-            spai_io::HostCsr h = spai_io::read_matrix_market(in);
+            spai_mm::HostCsr h = spai_mm::read_buffer(reinterpret_cast<const char *>(hbuf), static_cast<size_t>(fsize));
             auto m = std::make_unique<spai_mm_matrix_s>();
             m->rows = static_cast<int64_t>(h.rows);
             m->cols = static_cast<int64_t>(h.cols);
@@ -625,13 +496,14 @@ extern "C" int spai_mm_read(const char *path, int64_t device_min_lines, spai_mm_
         for (long long ln : fbl) {
             if (hfirst[0] != ULLONG_MAX && static_cast<unsigned long long>(ln) > hfirst[0])
                 break;
-            std::istringstream coord(line_text(ln));
-            std::string r_, c_, vt;
-            coord >> r_ >> c_ >> vt;
+            const std::string text = line_text(ln);
+            const unsigned char *ls = reinterpret_cast<const unsigned char *>(text.data());
+            long long fbeg[3], fend[3];
+            spai_mm::split_fields(ls, static_cast<long long>(text.size()), fbeg, fend, 3);
             try {
-                fbv.push_back(host_value(vt, integer_field));
+                fbv.push_back(spai_mm::host_value(spai_mm::field_text(ls, fbeg[2], fend[2]), integer_field));
                 fb_lines_used.push_back(ln);
-            } catch (const FormatError &e) {
+            } catch (const std::runtime_error &e) {
                 host_err_line = ln;
                 host_err = e.what();
                 break;

@@ -201,3 +201,74 @@ def test_mm_reader_host_path_errors(built, tmp_path):
     with pytest.raises(spai_ir.SpaiError) as e:
         spai_ir.mm_read(tmp_path / "missing.mtx", 1 << 62)
     assert e.value.code == spai_ir.ERR_ARGUMENT
+
+
+BANNER = "%%MatrixMarket matrix coordinate real general\n"
+MM_ERRORS = [
+    ("", "Missing Matrix Market banner"),
+    ("%%MatrixMarket matrix coordinate real\n3 3 0\n", "Malformed Matrix Market banner"),
+    ("%%MatrixMarket matrix coordinate real general x\n3 3 0\n", "Extra field in Matrix Market line"),
+    ("%%MatrixMarket matrix array real general\n3 3 0\n", "Unsupported Matrix Market format"),
+    ("%%MatrixMarket matrix coordinate complex general\n3 3 0\n", "Unsupported Matrix Market format"),
+    ("%%matrixmarket matrix coordinate real general\n3 3 0\n", "Unsupported Matrix Market format"),
+    (BANNER, "Missing matrix dimensions"),
+    (BANNER + "% only a comment\n \t\r\n", "Missing matrix dimensions"),
+    (BANNER + "3 3\n", "Malformed matrix dimensions"),
+    (BANNER + "3 3 0 0\n", "Extra field in Matrix Market line"),
+    (BANNER + "3 x 0\n", "Expected a nonnegative integer dimension/index"),
+    (BANNER + "+3 3 0\n", "Expected a nonnegative integer dimension/index"),
+    (BANNER + "99999999999999999999 3 0\n", "Dimension/index exceeds size_t"),
+    (BANNER + "0 3 0\n", "Matrix dimensions must be positive"),
+    ("%%MatrixMarket matrix coordinate real symmetric\n3 4 0\n", "Symmetric matrix must be square"),
+    (BANNER + "3 3 2\n1 1 1\n", "Truncated coordinate data"),
+    (BANNER + "3 3 1\n1 1 1\n2 2 2\n", "Trailing coordinate data"),
+    (BANNER + "3 3 1\n1 1\n", "Malformed coordinate entry"),
+    (BANNER + "3 3 1\n\v\n", "Malformed coordinate entry"),
+    (BANNER + "3 3 1\n1 1 1 1\n", "Extra field in Matrix Market line"),
+    (BANNER + "3 3 1\n-1 1 1\n", "Expected a nonnegative integer dimension/index"),
+    (BANNER + "3 3 1\n1 18446744073709551616 1\n", "Dimension/index exceeds size_t"),
+    (BANNER + "3 3 1\n4 1 1\n", "Matrix Market index outside one-based dimensions"),
+    (BANNER + "3 3 1\n1 0 1\n", "Matrix Market index outside one-based dimensions"),
+    (BANNER + "3 3 1\n1 1 abc\n", "Invalid coordinate value"),
+    (BANNER + "3 3 1\n1 1 1e400\n", "Invalid coordinate value"),
+    (BANNER + "3 3 1\n1 1 1e-320\n", "Invalid coordinate value"),
+    (BANNER + "3 3 1\n1 1 1.5x\n", "Coordinate value must be finite and numeric"),
+    (BANNER + "3 3 1\n1 1 inf\n", "Coordinate value must be finite and numeric"),
+    (BANNER + "3 3 1\n1 1 nan\n", "Coordinate value must be finite and numeric"),
+    ("%%MatrixMarket matrix coordinate integer general\n3 3 1\n1 1 1.5\n",
+     "Integer field requires integer value tokens"),
+    ("%%MatrixMarket matrix coordinate integer general\n3 3 1\n1 1 1e3\n",
+     "Integer field requires integer value tokens"),
+]
+
+
+@pytest.mark.parametrize("text,message", MM_ERRORS)
+def test_mm_reader_host_path_error_contract(built, tmp_path, text, message):
+    """Every malformed-input case of the reference reader (src/cpu.cpp:105-161) gives its message
+    and the runtime_error class (SPAI_ERR_FORMAT, CLI exit 1) through the host reader."""
+    p = tmp_path / "e.mtx"
+    p.write_bytes(text.encode())
+    with pytest.raises(spai_ir.SpaiError) as e:
+        spai_ir.mm_read(p, 1 << 62)
+    assert e.value.code == spai_ir.ERR_FORMAT, (text, str(e.value))
+    assert str(e.value).endswith(": " + message), (text, str(e.value))
+
+
+def test_mm_reader_host_path_invalid_entries_and_edge_cases(built, tmp_path):
+    """A duplicate sum that overflows is an invalid entry (invalid_argument: SPAI_ERR_ARGUMENT, CLI
+    exit 2). Valid edge cases: CRLF line ends and tabs, no final newline, comment and blank lines
+    between entries, a zero duplicate sum dropped, symmetric mirrors, integer spellings."""
+    p = tmp_path / "d.mtx"
+    p.write_text(BANNER + "2 2 2\n1 1 1e308\n1 1 1e308\n")
+    with pytest.raises(spai_ir.SpaiError) as e:
+        spai_ir.mm_read(p, 1 << 62)
+    assert e.value.code == spai_ir.ERR_ARGUMENT and str(e.value).endswith(": Duplicate sum is nonfinite")
+    p.write_bytes(b"%%MatrixMarket matrix coordinate real symmetric\r\n% c\r\n3\t3 5\r\n"
+                  b"1 1 2.5\r\n\r\n3 1 -1\r\n % indented comment\n2 2 4\n3 3 1\n3 3 -1")
+    (n, ptr, idx, val), cols, _ = spai_ir.mm_read(p, 1 << 62)
+    assert n == 3 and cols == 3
+    assert ptr.tolist() == [0, 2, 3, 4]
+    assert idx.tolist() == [0, 2, 1, 0] and val.tolist() == [2.5, -1.0, 4.0, -1.0]
+    p.write_text("%%MatrixMarket matrix coordinate integer general\n2 2 3\n2 2 +7\n1 2 -3\n2 2 -07\n")
+    (n, ptr, idx, val), cols, _ = spai_ir.mm_read(p, 1 << 62)
+    assert ptr.tolist() == [0, 1, 1] and idx.tolist() == [1] and val.tolist() == [-3.0]
