@@ -44,7 +44,11 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--grid", type=int, default=128, help="cube side (128 = the benchmark system)")
-    ap.add_argument("--innercap", type=int, default=200)
+    ap.add_argument("--workload", choices=["cd3d", "irregular"], default="cd3d",
+                    help="cd3d: 3-D convection-diffusion (--grid^3, the benchmark system); irregular: the "
+                         "10^6 Zipf-row random system (eps 0.4, innercap 150)")
+    ap.add_argument("--n", type=int, default=1_000_000, help="irregular workload size")
+    ap.add_argument("--innercap", type=int, default=None, help="default 200 (cd3d) / 150 (irregular)")
     ap.add_argument("--fp64-steps", type=int, default=1)
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
@@ -56,6 +60,26 @@ def parse():
                     help="profile run: drive the refinement loop from the host instead of one CUDA graph "
                          "(ncu profiles no kernel node of a graph with conditional nodes)")
     return ap.parse_args()
+
+
+def workload(args):
+    """(system, epsilon, description, data) of the selected workload; sets args.innercap's default."""
+    from spai_ir import matrices as M
+
+    if args.workload == "irregular":
+        if args.innercap is None:
+            args.innercap = 150
+        system = M.irregular(args.n, seed=0)
+        desc = ("mixed SPAI-GMRES-IR, irregular system n=%d (off-diagonal counts Zipf(1.5) in [1,256], "
+                "N(0,1) values, diagonal 1.1 x row sum), nnz=%d, eps 0.4, alpha ceil(n/8), beta 8, innercap %d, "
+                "outercap 20, BE<=1e-12" % (system[0], len(system[3]), args.innercap))
+        return system, 0.4, desc, "synthetic (seeded irregular Zipf-row system, matrices.py)"
+    if args.innercap is None:
+        args.innercap = 200
+    system = M.convection_diffusion_3d(args.grid)
+    desc = ("mixed SPAI-GMRES-IR, 3-D convection-diffusion %d^3 (n=%d, nnz=%d), eps 0.3, alpha ceil(n/8), "
+            "beta 8, innercap %d, outercap 20, BE<=1e-12" % (args.grid, system[0], len(system[3]), args.innercap))
+    return system, 0.3, desc, "synthetic (seeded %d^3 upwind convection-diffusion, matrices.py)" % args.grid
 
 
 def profile_run(args):
@@ -81,9 +105,9 @@ def profile_run(args):
                           "solve_ms": reps[0]["solve_ms"], "converged": sum(r["converged"] for r in reps)}))
         return
 
-    system = M.convection_diffusion_3d(args.grid)
+    system, eps, _, _ = workload(args)
     n = system[0]
-    opts = spai_ir.cli_options(n, args.profile_run, innercap=args.innercap, be_tolerance=BE_TARGET,
+    opts = spai_ir.cli_options(n, args.profile_run, epsilon=eps, innercap=args.innercap, be_tolerance=BE_TARGET,
                                flags=spai_ir.FLAG_NO_GRAPH if args.no_graph else 0)
     with spai_ir.Handle(system, args.profile_run) as h:
         rb = h.build(opts)
@@ -192,10 +216,10 @@ def run_ours(args, rank, world, local):
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     stream = torch.cuda.Stream(device=dev)  # the library launches on this stream
-    system = M.convection_diffusion_3d(args.grid)
+    system, eps, desc, data = workload(args)
     n, ptr, idx, val = system
     b_host = M.equal_rhs(n)
-    opts = {p: spai_ir.cli_options(n, p, innercap=args.innercap, be_tolerance=BE_TARGET)
+    opts = {p: spai_ir.cli_options(n, p, epsilon=eps, innercap=args.innercap, be_tolerance=BE_TARGET)
             for p in ("mixed", "f64")}
     b_dev = torch.from_numpy(b_host).to(dev)
     x_dev = torch.zeros(n, dtype=torch.float64, device=dev)
@@ -282,7 +306,8 @@ def run_ours(args, rank, world, local):
     p_mixed = handles["mixed"].preconditioner()
     for hh in handles.values():
         hh.close()
-    return {"p": p_mixed, "ms": ms_mixed, "rb": rb_m, "rs": rs_m, "launches": launches, "e2e": e2e, "h2d": h2d,
+    return {"system": system, "eps": eps, "desc": desc, "data": data,
+            "p": p_mixed, "ms": ms_mixed, "rb": rb_m, "rs": rs_m, "launches": launches, "e2e": e2e, "h2d": h2d,
             "d2h": d2h, "fp64": fp64, "roofline": roofline, "clocks": clocks.summary(), "n": n,
             "nnz": len(val)}
 
@@ -317,7 +342,7 @@ def run_batched(steps=2, warmup=1):
                     "reference algorithm (the oracle fails the same systems)"}
 
 
-def cpu_estimate(grid, fits_total, iter_counts, threads, precision="mixed", p_system=None):
+def cpu_estimate(system, eps, iter_counts, threads, precision="mixed", p_system=None):
     """Oracle cost on a bounded sample, extrapolated to the full solve."""
     import numpy as np
 
@@ -325,11 +350,10 @@ def cpu_estimate(grid, fits_total, iter_counts, threads, precision="mixed", p_sy
     import oracle as O
     from spai_ir import matrices as M
 
-    system = M.convection_diffusion_3d(grid)
     n = system[0]
     rng = np.random.default_rng(0)
     cols = np.sort(rng.choice(n, size=min(n, 32768), replace=False))
-    sec, fits = O.spai_sample_seconds(system, cols, epsilon=0.3, alpha=(n + 7) // 8, beta=8,
+    sec, fits = O.spai_sample_seconds(system, cols, epsilon=eps, alpha=(n + 7) // 8, beta=8,
                                       precision=precision, threads=threads)
     spai_total = sec / len(cols) * n
     # GMRES cost model t(K) = a K + b K^2 / 2 from two fixed-length runs (tau = 1e-30, so every
@@ -369,28 +393,25 @@ def run_reference(args, threads):
     from spai_ir import matrices as M
 
     O.set_threads(threads)
-    system = M.convection_diffusion_3d(args.grid)
+    system, eps, desc, data = workload(args)
     n = system[0]
     b = M.equal_rhs(n)
     t0 = time.perf_counter()
-    x, r = O.ir(system, b, precision="mixed", innercap=args.innercap, be_tolerance=BE_TARGET)
+    x, r = O.ir(system, b, precision="mixed", epsilon=eps, innercap=args.innercap, be_tolerance=BE_TARGET)
     ms = (time.perf_counter() - t0) * 1e3
     c1 = M.convection_diffusion_2d(64)
     t1 = time.perf_counter()
     _, r1 = O.ir(c1, M.equal_rhs(c1[0]), precision="f64", outercap=20, innercap=0)
     c1_ms = (time.perf_counter() - t1) * 1e3
-    sample = ("one complete mixed solve of the %d^3 system by the oracle: SPAI %.1f s on %d threads, "
+    sample = ("one complete mixed solve of the workload by the oracle: SPAI %.1f s on %d threads, "
               "GMRES + refinement %.1f s on 1 thread (%d outer steps, %d Arnoldi steps, backward error %.2e)"
-              % (args.grid, r["spai_seconds"], threads, r["refine_seconds"], r["outer_steps"],
+              % (r["spai_seconds"], threads, r["refine_seconds"], r["outer_steps"],
                  r["inner_iterations"], r["nbe"]))
     return {"impl": "reference", "metric": METRIC, "value": round(ms, 1), "unit": "ms",
             "n_gpus": args.gpus, "steps": 1, "warmup": 0, "ms_per_step": round(ms, 1),
             "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
-            "data": "synthetic (seeded %d^3 upwind convection-diffusion, matrices.py)" % args.grid,
-            "config": {"workload": "mixed SPAI-GMRES-IR, 3-D convection-diffusion %d^3 (n=%d, nnz=%d), eps 0.3, "
-                                   "alpha ceil(n/8), beta 8, innercap %d, outercap 20, BE<=1e-12"
-                                   % (args.grid, n, len(system[3]), args.innercap),
-                       "l2": "host memory (CPU run)"},
+            "data": data,
+            "config": {"workload": desc, "l2": "host memory (CPU run)"},
             "cpu_baseline": {"value": round(ms, 1), "unit": "ms", "cores": threads, "kind": "port",
                              "sample": sample},
             "e2e": {"value": round(ms, 1), "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -411,6 +432,9 @@ def main():
     if args.profile_run:
         profile_run(args)
         return
+    if args.workload == "irregular":  # the binary64 SPAI of the heavy columns takes minutes
+        args.no_fp64 = True
+        args.no_batched = True
     rank, world, local = dist_env()
     if world > 1 and args.impl == "ours":
         import torch
@@ -433,8 +457,7 @@ def main():
     if not args.no_cpu:
         iters_est = [res["rs"]["inner_iterations"] // max(res["rs"]["inner_attempts"], 1)] * max(
             res["rs"]["inner_attempts"], 1)
-        ms_cpu, sample, parts = cpu_estimate(args.grid, res["rb"]["spai_fits"], iters_est, threads,
-                                             p_system=res["p"])
+        ms_cpu, sample, parts = cpu_estimate(res["system"], res["eps"], iters_est, threads, p_system=res["p"])
         cpu = {"value": round(ms_cpu, 1), "unit": "ms", "cores": threads, "kind": "port", "sample": sample,
                "extrapolated": True,
                "note": "bounded sample scaled to one solve; the reference arm (--impl reference) times a "
@@ -443,10 +466,8 @@ def main():
         "metric": METRIC, "value": round(res["ms"], 2), "unit": "ms", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(res["ms"], 2),
         "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
-        "data": "synthetic (seeded 128^3 upwind convection-diffusion, matrices.py)",
-        "config": {"workload": "mixed SPAI-GMRES-IR, 3-D convection-diffusion %d^3 (n=%d, nnz=%d), eps 0.3, "
-                               "alpha ceil(n/8), beta 8, innercap %d, outercap 20, BE<=1e-12"
-                               % (args.grid, res["n"], res["nnz"], args.innercap),
+        "data": res["data"],
+        "config": {"workload": res["desc"],
                    "parallelism": "replicas" if world > 1 else "single GPU",
                    "l2": "inputs larger than L2 (A 175 MB, Krylov basis GBs); no flush"},
         "e2e": {"value": round(res["e2e"], 2), "unit": "ms", "h2d_bytes_per_step": res["h2d"],

@@ -25,6 +25,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -964,8 +965,13 @@ template <class T, class TO> struct IrEngine {
         nblk_dots = std::min(ntiles, sms);
         ctl = arena.alloc<Ctl>(1);
         cudaStream_t setup_st = nullptr;
-        sa = build_sell(arena, ai, sms, setup_st);
-        sp = build_sell(arena, pp, sms, setup_st);
+        // Slice order by the row-length profile (sorted for heavy tails); SPAI_SELL_ORDER=0/1
+        // forces natural/sorted rows (equivalence checks and tuning sweeps).
+        int sell_order = -1;
+        if (const char *e = std::getenv("SPAI_SELL_ORDER"))
+            sell_order = std::atoi(e);
+        sa = build_sell(arena, ai, sms, setup_st, sell_order);
+        sp = build_sell(arena, pp, sms, setup_st, sell_order);
         SPAI_CUDA(cudaStreamSynchronize(setup_st));
         const size_t vcount = static_cast<size_t>(ntiles) * (cap + 1) * R;
         {

@@ -421,8 +421,17 @@ __device__ int grp_least_squares(const Grp &g, T *R, T *rhs, int m, int q, T *co
         } else {
             // chain over the column's nonzeros (compacted into v, which is rewritten below)
             const int nz = grp_compact_nonzero(g, R + static_cast<long long>(j) * q + j, m - j, q, v);
-            if (lane == 0)
+            if (lane == 0) {
+                if (clk && clk->out) {
+                    // tuning aid: how many groups' chains the warp runs together (lanes active here)
+                    const unsigned am = __activemask();
+                    if (static_cast<int>(threadIdx.x & 31) == __ffs(am) - 1) {
+                        atomicAdd(clk->out + kPhCount, static_cast<unsigned long long>(__popc(am)));
+                        atomicAdd(clk->out + kPhCount + 1, 1ull);
+                    }
+                }
                 length = norm_chain(v, nz, 1);
+            }
             length = g.shfl(length, 0);
             g.sync();
         }
@@ -1231,8 +1240,8 @@ void SpaiBuilder<T>::construct(const DeviceCsr<T> &a, const SpaiParams &prm, cud
         SPAI_CUDA(cudaMemsetAsync(top, 0, sizeof(unsigned long long), st));
         unsigned long long *phase = nullptr;
         if (trace) {
-            phase = arena.alloc<unsigned long long>(kPhCount);
-            SPAI_CUDA(cudaMemsetAsync(phase, 0, sizeof(unsigned long long) * kPhCount, st));
+            phase = arena.alloc<unsigned long long>(kPhCount + 2);
+            SPAI_CUDA(cudaMemsetAsync(phase, 0, sizeof(unsigned long long) * (kPhCount + 2), st));
         }
         ColumnArgs<T> args{n, a.rp, a.ci, a.val, tp, ti, d, static_cast<T>(prm.epsilon), prm.alpha,
                            prm.beta, out.col_status, out.col_fits, out.col_growths, out.col_clamps,
@@ -1277,17 +1286,18 @@ void SpaiBuilder<T>::construct(const DeviceCsr<T> &a, const SpaiParams &prm, cud
             in_list = out_list;
         }
         if (trace && phase) {
-            unsigned long long hp[kPhCount];
+            unsigned long long hp[kPhCount + 2];
             SPAI_CUDA(cudaMemcpy(hp, phase, sizeof(hp), cudaMemcpyDeviceToHost));
             double tot = 0;
-            for (unsigned long long v : hp)
-                tot += static_cast<double>(v);
+            for (int i = 0; i < kPhCount; ++i)
+                tot += static_cast<double>(hp[i]);
             static const char *names[kPhCount] = {"shadow", "qr_other", "residual", "candidates",
                                                   "scores", "select", "qr_norms", "qr_update"};
             std::fprintf(stderr, "spai fit phases (lane-0 cycles, all tiers):");
             for (int i = 0; i < kPhCount; ++i)
                 std::fprintf(stderr, " %s %.1f%%", names[i], tot > 0 ? 100.0 * hp[i] / tot : 0.0);
-            std::fprintf(stderr, "\n");
+            std::fprintf(stderr, "; column-length chains per warp issue %.2f\n",
+                         hp[kPhCount + 1] ? static_cast<double>(hp[kPhCount]) / hp[kPhCount + 1] : 0.0);
         }
         int h_err = 0;
         SPAI_CUDA(cudaMemcpyAsync(&h_err, err, sizeof(int), cudaMemcpyDeviceToHost, st));
