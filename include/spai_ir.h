@@ -272,11 +272,24 @@ int spai_history(spai_handle *h, spai_outer_record *outer, int64_t max_outer, in
 
 /* Per-kernel-class timing of refinement solves (CUDA events on the handle's stream around each
  * launch). Classes: 0 SpMV with A (basis vector gathered), 1 SpMV with P, 2 Gram-Schmidt pass 1
- * (dots), 3 pass 2 (update + dots), 4 pass 3 (reorthogonalisation, only when it runs). enable != 0 resets and starts recording; read returns the accumulated
+ * (dots), 3 pass 2 (update + dots; with the lagged second projection also the correction of the
+ * previous vector), 4 pass 3 (reorthogonalisation; only in the three-pass form and only when it
+ * runs). enable != 0 resets and starts recording; read returns the accumulated
  * device milliseconds, launch count and algorithmic bytes of one class. No reference
  * counterpart (the reference only kept host wall-clock telemetry, src/cuda_spai.cu:19-38). */
 int spai_profile(spai_handle *h, int32_t enable);
 int spai_profile_read(spai_handle *h, int32_t cls, double *ms, int64_t *launches, double *bytes);
+
+/* Choices of the autotuner for the handle's last build and solve set-up (no reference
+ * counterpart: the reference's launch policy is fixed, e.g. 8 slot streams in
+ * src/cuda_spai.cu:575-577). out[0] lanes per column group and out[1] workspace bytes per group
+ * of the SPAI's first workspace tier; out[2] = 1 when the autotuner chose them (first-tier
+ * candidates timed on a column sample, cached per sparsity profile for the process), 0 for the
+ * profile default or an override; out[3] / out[4] slice order of the Krylov SpMV with the inner
+ * A / with P (0 natural rows, 1 rows sorted by length, -1 no solve set up yet).
+ * ms (optional, 2 doubles): the chosen pair's and the default pair's time on the sample (NaN
+ * when not tuned). Returns SPAI_OK or an error code. */
+int spai_tuning(spai_handle *h, int32_t *out, double *ms);
 
 /* Backward error of a given x with no device allocation (no counterpart in the reference).
  * For callers that cannot call cudaMalloc where they need this check: applications whose device
@@ -297,9 +310,10 @@ int spai_profile_read(spai_handle *h, int32_t cls, double *ms, int64_t *launches
 int spai_backward_error_noalloc(spai_handle *h, const double *d_b, const double *d_x,
                                 double *d_out, void *stream);
 
-/* The device's correctly rounded hypot on host arrays (precision 0: binary64, otherwise binary32
- * on the operands rounded to binary32, widened on return): the function every SPAI column norm
- * chain calls, exposed so that it can be checked against an independent implementation.
+/* The device's correctly rounded hypot on host arrays, exposed so that it can be checked against
+ * an independent implementation. precision 0: binary64 hypot; 1: binary32 hypot on the operands
+ * rounded to binary32 (widened on return); 2 / 3: the binary64 / binary32 step of the SPAI norm
+ * chains from the running norm |a|, which must give the same bits as 0 / 1.
  * Returns SPAI_OK or an error code. No reference counterpart. */
 int spai_hypot_device(int32_t precision, int64_t count, const double *a, const double *b, double *out);
 

@@ -549,6 +549,8 @@ int spai_build(spai_handle *h, const spai_options *opt, spai_report *rep) {
         prm.ws_bytes_per_warp = std::atoi(e);
     if (const char *e = std::getenv("SPAI_QCAP"))
         prm.first_qcap = std::atoi(e);
+    if (const char *e = std::getenv("SPAI_TUNE"))
+        prm.tune = std::atoi(e) != 0;
     prm.epsilon = opt->epsilon;
     // Every form follows the reference's sequential arithmetic bit for bit by default; the
     // group-parallel variant (parallel norms and mean, hashed candidate sets) is opt-in.
@@ -970,6 +972,42 @@ int spai_profile_read(spai_handle *h, int32_t cls, double *ms, int64_t *launches
         *launches = h->prof.launches[cls];
     if (bytes)
         *bytes = h->prof.bytes[cls];
+    return SPAI_OK;
+    API_END
+}
+
+int spai_tuning(spai_handle *h, int32_t *out, double *ms) {
+    API_BEGIN
+    if (!h || !out)
+        return fail(SPAI_ERR_ARGUMENT, "spai_tuning: null argument");
+    const bool f64 = h->precision == SPAI_PREC_F64;
+    const int G = f64 ? h->s64.group_lanes : h->s32.group_lanes;
+    const int ws = f64 ? h->s64.ws_bytes : h->s32.ws_bytes;
+    const bool tuned = f64 ? h->s64.tuned : h->s32.tuned;
+    int oa = -1, op = -1;
+    auto orders = [&](const auto &e) {
+        if (e.n > 0) {
+            oa = e.sa.sorted() ? 1 : 0;
+            op = e.sp.sorted() ? 1 : 0;
+        }
+    };
+    if (h->engine_cap >= 0) {
+        if (h->precision == SPAI_PREC_F64)
+            orders(h->e64);
+        else if (h->precision == SPAI_PREC_MIXED)
+            orders(h->emix);
+        else
+            orders(h->e32);
+    }
+    out[0] = G;
+    out[1] = ws;
+    out[2] = tuned ? 1 : 0;
+    out[3] = oa;
+    out[4] = op;
+    if (ms) {
+        ms[0] = tuned ? (f64 ? h->s64.tune_sample_ms : h->s32.tune_sample_ms) : NAN;
+        ms[1] = tuned ? (f64 ? h->s64.tune_default_ms : h->s32.tune_default_ms) : NAN;
+    }
     return SPAI_OK;
     API_END
 }

@@ -294,6 +294,91 @@ template <class T> SPAI_HD T cr_hypot(T a, T b) {
     return cr_hypot_general(x, y);
 }
 
+#ifdef __CUDACC__
+// One step of a norm chain, c <- cr_hypot(c, a) with c >= 0, carrying c's square as the
+// unevaluated exact sum cc + cce (error-free product). The square of the new value is exactly the
+// product the acceptance test of the step forms anyway, so the next step starts from the sum of
+// squares directly: the chain's dependency path is one addition, one square root, one exact
+// product and the test, with no ordering, scaling or unscaling of the operands.
+//
+// The test is the one of cr_hypot_fast on unscaled operands. Both c and |a| lie in
+// [2^-40, 2^40] on the fast path, so every square and every product error term is a normal
+// number (no bits lost), and the computed remainder R of (c^2 + a^2) - c'^2 is within about
+// 2^-48 c'^2 of the exact one, far inside the 2^-16 margin of the threshold. Outside that range,
+// and when the test rejects, the step calls cr_hypot; when |a| < 2^-14 c the correctly rounded
+// value is c itself (the rule cr_hypot applies too). Every step therefore returns exactly
+// cr_hypot(c, a), bit for bit, for every input including zeros, subnormals, infinities and NaNs.
+template <class T> struct NormChain {
+    T c = 0, cc = 0, cce = 0;
+};
+__device__ __forceinline__ void norm_chain_step(NormChain<float> &st, float a) {
+    const float y = fabsf(a);
+    const int fy = static_cast<int>(__float_as_uint(y) >> 23);
+    const int fc = static_cast<int>(__float_as_uint(st.c) >> 23);
+    if (fc - fy > 14)
+        return;
+    if (static_cast<unsigned>(fc - 87) <= 80u && static_cast<unsigned>(fy - 87) <= 80u) {
+        const float yy = __fmul_rn(y, y), yye = __fmaf_rn(y, y, -yy);
+        const float s = __fadd_rn(st.cc, yy);
+        const float c = __fsqrt_rn(s);
+        const float p = __fmul_rn(c, c), pe = __fmaf_rn(c, c, -p);
+        const float bv = __fsub_rn(s, st.cc), av = __fsub_rn(s, bv);
+        const float sl = __fadd_rn(__fsub_rn(st.cc, av), __fsub_rn(yy, bv));
+        const float r = __fadd_rn(__fsub_rn(s, p), __fadd_rn(__fsub_rn(sl, pe), __fadd_rn(st.cce, yye)));
+        const unsigned bc = __float_as_uint(c);
+        const unsigned hb = (bc & 0x7f800000u) - (24u << 23) - ((bc & 0x007fffffu) == 0 ? (1u << 23) : 0u);
+        const float thr = __fmul_rn(__fmul_rn(__fadd_rn(c, c), __uint_as_float(hb)), 0.9999847412109375f);
+        if (fabsf(r) < thr) {
+            st.c = c;
+            st.cc = p;
+            st.cce = pe;
+            return;
+        }
+    }
+    st.c = cr_hypot<float>(st.c, y);
+    st.cc = __fmul_rn(st.c, st.c);
+    st.cce = __fmaf_rn(st.c, st.c, -st.cc);
+}
+__device__ __forceinline__ void norm_chain_step(NormChain<double> &st, double a) {
+    const double y = fabs(a);
+    const int fy = static_cast<int>(static_cast<unsigned long long>(__double_as_longlong(y)) >> 52);
+    const int fc = static_cast<int>(static_cast<unsigned long long>(__double_as_longlong(st.c)) >> 52);
+    if (fc - fy > 30)
+        return;
+    if (static_cast<unsigned>(fc - 623) <= 800u && static_cast<unsigned>(fy - 623) <= 800u) {
+        const double yy = __dmul_rn(y, y), yye = __fma_rn(y, y, -yy);
+        const double s = __dadd_rn(st.cc, yy);
+        const double c = __dsqrt_rn(s);
+        const double p = __dmul_rn(c, c), pe = __fma_rn(c, c, -p);
+        const double bv = __dsub_rn(s, st.cc), av = __dsub_rn(s, bv);
+        const double sl = __dadd_rn(__dsub_rn(st.cc, av), __dsub_rn(yy, bv));
+        const double r = __dadd_rn(__dsub_rn(s, p), __dadd_rn(__dsub_rn(sl, pe), __dadd_rn(st.cce, yye)));
+        const unsigned long long bc = static_cast<unsigned long long>(__double_as_longlong(c));
+        const unsigned long long hb = (bc & 0x7ff0000000000000ull) - (53ull << 52) -
+                                      ((bc & 0x000fffffffffffffull) == 0 ? (1ull << 52) : 0ull);
+        const double thr = __dmul_rn(__dmul_rn(__dadd_rn(c, c), __longlong_as_double(static_cast<long long>(hb))),
+                                     0.99999999999909050530);
+        if (fabs(r) < thr) {
+            st.c = c;
+            st.cc = p;
+            st.cce = pe;
+            return;
+        }
+    }
+    st.c = cr_hypot<double>(st.c, y);
+    st.cc = __dmul_rn(st.c, st.c);
+    st.cce = __fma_rn(st.c, st.c, -st.cc);
+}
+// The chain step from a running norm c >= 0 (its square formed here), for tests.
+template <class T> __device__ __forceinline__ T norm_chain_step_from(T c, T a) {
+    NormChain<T> st;
+    st.c = c;
+    em_two_prod(c, c, st.cc, st.cce);
+    norm_chain_step(st, a);
+    return st.c;
+}
+#endif
+
 
 
 } // namespace spai

@@ -38,6 +38,7 @@ struct Ctl {
     int verifications; // candidate checks run in this solve
     int reorth;        // this step needs the second Gram-Schmidt pass (DGKS criterion)
     int reorth_count;  // second passes run in this solve
+    int lag_pending;   // lagged Gram-Schmidt: the newest basis vector awaits its second projection
     double wnorm;      // ||P A v_k|| before orthogonalisation
     double be, cbe, rinf, xinf, bscale, anorm_inf, binf;
     double inner_scale; // power of two applied to the correction right-hand side

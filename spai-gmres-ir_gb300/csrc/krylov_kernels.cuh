@@ -336,6 +336,7 @@ template <class T> __global__ void gmres_start_kernel(Ctl *ctl, const T *orig, i
     if (threadIdx.x != 0 || !ctl->outer_active)
         return;
     ctl->k = 0;
+    ctl->lag_pending = 0;
     ctl->triggered = 0;
     ctl->breakdown = 0;
     ctl->converged = 0;
@@ -708,6 +709,55 @@ void launch_sell(const DeviceSell<T> &m, VecRef<T> x, VecRef<T> y, const int *ga
     SPAI_LAUNCH("sell_spmv_kernel");
 }
 
+template <class T> __global__ void fill_kernel(int n, T *x, T v) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        x[i] = v;
+}
+
+// Autotuned slice order of a Krylov SpMV operand. With order < 0 (no override) the natural
+// layout is built first; when it pads the matrix by more than 5 % (uneven row lengths), the
+// length-sorted layout is built too and both are timed on one SpMV each (best of three, CUDA
+// events, on a vector of ones), and the faster is kept. Both layouts sum every row in the same
+// order, so the choice changes speed only. The discarded layout stays in the arena (the next
+// setup of the same shape reuses its buffers).
+template <class T>
+DeviceSell<T> tuned_sell(DeviceArena &arena, const DeviceCsr<T> &m, int sms, cudaStream_t st, int order) {
+    if (order >= 0)
+        return build_sell(arena, m, sms, st, order);
+    DeviceSell<T> nat = build_sell(arena, m, sms, st, 0);
+    SPAI_CUDA(cudaStreamSynchronize(st));
+    if (nat.entries * 20 <= static_cast<long long>(m.nnz) * 21 + 20LL * 32 || m.n < 4096)
+        return nat;
+    DeviceSell<T> srt = build_sell(arena, m, sms, st, 1);
+    T *x = arena.alloc<T>(m.n);
+    T *y = arena.alloc<T>(m.n);
+    fill_kernel<T><<<grid_for(m.n, kBlock, sms * 8), kBlock, 0, st>>>(m.n, x, T(1));
+    SPAI_LAUNCH("fill_kernel");
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    SPAI_CUDA(cudaEventCreate(&e0));
+    SPAI_CUDA(cudaEventCreate(&e1));
+    auto time_one = [&](const DeviceSell<T> &sm) {
+        float best = INFINITY;
+        for (int r = 0; r < 3; ++r) {
+            SPAI_CUDA(cudaEventRecord(e0, st));
+            launch_sell<T>(sm, VecRef<T>{x, 0, nullptr, 0}, VecRef<T>{y, 0, nullptr, 0}, nullptr, sms, st);
+            SPAI_CUDA(cudaEventRecord(e1, st));
+            SPAI_CUDA(cudaEventSynchronize(e1));
+            float ms = 0;
+            SPAI_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+            best = std::min(best, ms);
+        }
+        return best;
+    };
+    const float t_nat = time_one(nat), t_srt = time_one(srt);
+    SPAI_CUDA(cudaEventDestroy(e0));
+    SPAI_CUDA(cudaEventDestroy(e1));
+    if (std::getenv("SPAI_TRACE"))
+        std::fprintf(stderr, "sell tune: n=%d nnz=%d natural %lld entries %.3f ms, sorted %lld entries %.3f ms\n", m.n,
+                     m.nnz, nat.entries, t_nat, srt.entries, t_srt);
+    return t_srt < t_nat ? srt : nat;
+}
+
 // Optional per-kernel-class timing: CUDA events recorded on the solve stream around each
 // launch of the Arnoldi kernels. Launch records of speculative steps past the end of a GMRES
 // solve are discarded using the solve's iteration count.
@@ -778,6 +828,10 @@ template <class T, class TO> struct IrEngine {
     T *V = nullptr, *sc = nullptr, *w = nullptr, *t = nullptr, *rhs = nullptr, *pb = nullptr, *cand = nullptr,
       *ax = nullptr, *pax = nullptr, *H = nullptr, *cs = nullptr, *sn = nullptr, *g = nullptr,
       *y = nullptr, *h1 = nullptr, *h2 = nullptr, *part = nullptr, *scal = nullptr;
+    // Lagged second projection: projections, pending correction, its Hessenberg image and the
+    // unrotated Hessenberg (see cgs_tiles.cuh).
+    T *dl = nullptr, *cpend = nullptr, *ecorr = nullptr, *Hu = nullptr;
+    bool lag = false; // two basis reads per Arnoldi step (every step of the solve streams)
     TO *r = nullptr, *xn = nullptr;
     NormPart *npart = nullptr;
     DiagPart *dpart = nullptr;
@@ -827,11 +881,11 @@ template <class T, class TO> struct IrEngine {
 
     // Kernel nodes executed by the last graph solve, from the device loop counters: 4 init
     // nodes; per GMRES solve 8 start nodes (7 with right preconditioning) and 6 update/residual
-    // nodes; per Arnoldi step 7 passes, 2 condition sets and the decision; per candidate
-    // verification 6 (5 with right preconditioning).
+    // nodes; per Arnoldi step 7 passes (6 with the lagged Gram-Schmidt), 2 condition sets and
+    // the decision; per candidate verification 6 (5 with right preconditioning).
     long long graph_kernels(const Ctl &c) const {
         const long long steps = static_cast<long long>(c.guard) + c.inner_attempts;
-        return 4 + (right ? 13LL : 14LL) * c.inner_attempts + 10LL * steps +
+        return 4 + (right ? 13LL : 14LL) * c.inner_attempts + (lag ? 9LL : 10LL) * steps +
                (right ? 5LL : 6LL) * c.verifications;
     }
 
@@ -965,13 +1019,13 @@ template <class T, class TO> struct IrEngine {
         nblk_dots = std::min(ntiles, sms);
         ctl = arena.alloc<Ctl>(1);
         cudaStream_t setup_st = nullptr;
-        // Slice order by the row-length profile (sorted for heavy tails); SPAI_SELL_ORDER=0/1
+        // Slice order timed per operand when the natural layout pads (tuned_sell); SPAI_SELL_ORDER=0/1
         // forces natural/sorted rows (equivalence checks and tuning sweeps).
         int sell_order = -1;
         if (const char *e = std::getenv("SPAI_SELL_ORDER"))
             sell_order = std::atoi(e);
-        sa = build_sell(arena, ai, sms, setup_st, sell_order);
-        sp = build_sell(arena, pp, sms, setup_st, sell_order);
+        sa = tuned_sell(arena, ai, sms, setup_st, sell_order);
+        sp = tuned_sell(arena, pp, sms, setup_st, sell_order);
         SPAI_CUDA(cudaStreamSynchronize(setup_st));
         const size_t vcount = static_cast<size_t>(ntiles) * (cap + 1) * R;
         {
@@ -997,6 +1051,13 @@ template <class T, class TO> struct IrEngine {
         SPAI_CUDA(cudaFuncSetAttribute(cgs_pass_kernel<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
         SPAI_CUDA(cudaFuncSetAttribute(cgs_pass_kernel<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
         SPAI_CUDA(cudaFuncSetAttribute(cgs_pass_kernel<T, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        SPAI_CUDA(cudaFuncSetAttribute(cgs_pass_kernel<T, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        SPAI_CUDA(cudaFuncSetAttribute(cgs_pass_kernel<T, 5>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        // The lagged passes need every step to stream whole tiles (k + 2 <= stage_segs for
+        // k < cap); SPAI_CGS_LAG=0 keeps the three-pass form (comparisons).
+        lag = cap + 1 <= stage_segs && !cgs_acc_global<T>(cap);
+        if (const char *e = std::getenv("SPAI_CGS_LAG"))
+            lag = lag && std::atoi(e) != 0;
         w = arena.alloc<T>(ld);
         SPAI_CUDA(cudaMemset(w, 0, sizeof(T) * ld));
         t = arena.alloc<T>(ld);
@@ -1017,6 +1078,10 @@ template <class T, class TO> struct IrEngine {
         y = arena.alloc<T>(cap + 1);
         h1 = arena.alloc<T>(cap + 2);
         h2 = arena.alloc<T>(cap + 2);
+        dl = arena.alloc<T>(cap + 2);
+        cpend = arena.alloc<T>(cap + 2);
+        ecorr = arena.alloc<T>(cap + 2);
+        Hu = arena.alloc<T>(static_cast<size_t>(hld) * (cap + 1));
         part = arena.alloc<T>(static_cast<size_t>(std::max(nblk_dots, nblk_vec)) * (cap + 2));
         npart = arena.alloc<NormPart>(std::max(nblk_dots, nblk_vec));
         dpart = arena.alloc<DiagPart>(std::max(nblk_dots, nblk_vec));
@@ -1033,7 +1098,7 @@ template <class T, class TO> struct IrEngine {
     CgsArgs<T> cgs_args() const {
         return CgsArgs<T>{n, basis(), w, h1, h2, H, cs, sn, g, sc, hld, ctl,
                           CgsScratch{cgs_dots, cgs_norms, counters + kSlotDots}, always_reorth ? 1 : 0,
-                          stage_segs, cgs_gacc, cgs_gcf};
+                          stage_segs, cgs_gacc, cgs_gcf, dl, cpend, ecorr, Hu};
     }
     size_t cgs_smem() const {
         return cgs_dyn;
@@ -1087,6 +1152,20 @@ template <class T, class TO> struct IrEngine {
         });
         const size_t smem = cgs_smem();
         const CgsArgs<T> args = cgs_args();
+        if (lag) {
+            // Dots (reads W_0..W_k and z), then update with the pending correction of W_k (reads
+            // the same, writes W_k and W_{k+1}).
+            timed(st, kClsDots, vec_bytes(kk + 2), [&] {
+                cgs_pass_kernel<T, 4><<<nblk_dots, kCgsThreads, smem, st>>>(args);
+                SPAI_LAUNCH("cgs_pass_kernel<4>");
+            });
+            timed(st, kClsUpdate, vec_bytes(kk + 4), [&] {
+                cgs_pass_kernel<T, 5><<<nblk_dots, kCgsThreads, smem, st>>>(args);
+                SPAI_LAUNCH("cgs_pass_kernel<5>");
+            });
+            launches += 4;
+            return;
+        }
         timed(st, kClsDots, vec_bytes(kk + 2), [&] {
             cgs_pass_kernel<T, 1><<<nblk_dots, kCgsThreads, smem, st>>>(args);
             SPAI_LAUNCH("cgs_pass_kernel<1>");

@@ -26,6 +26,9 @@
 #include <cstdlib>
 
 #include <algorithm>
+#include <map>
+#include <mutex>
+#include <tuple>
 #include <vector>
 
 namespace spai {
@@ -354,52 +357,23 @@ __device__ T grp_norm(const Grp &g, const T *x, int m, long long stride) {
 // Householder least squares with normalised reflectors, src/spai.cpp:30-98. R is destroyed,
 // rhs is transformed, coef receives the solution. Returns a SpaiStatus code.
 // The reference's left-to-right hypot chain over count elements (stride apart), one correctly
-// rounded hypot per step. (Speculative and software-pipelined variants of this chain, with the
-// exactness test moved off the dependency path, measured slower on the 128^3 system: 465-541 ms
-// against 388-401 ms for the whole SPAI.)
+// rounded hypot per step, each step carrying the running value's exact square forward
+// (norm_chain_step: bit-identical to cr_hypot). Measured alternatives on the 128^3 system, all
+// slower: speculative and software-pipelined variants with the exactness test moved off the
+// dependency path (465-541 ms against 388-401 ms for the whole SPAI), chains over the column's
+// compacted nonzeros (443 ms: after the first reflectors the reduced columns are mostly filled
+// in, so the ballot/compaction costs more than the skipped zero steps save), and an explicit
+// one-ahead load of the next element (453 ms).
 template <class T> __device__ __forceinline__ T norm_chain(const T *x, int count, int stride) {
-    T r = 0;
-    // The next element is loaded before the current step, so its shared-memory latency overlaps
-    // the hypot instead of lengthening the dependency chain.
-    T next = count > 0 ? x[0] : T(0);
-    for (int i = 0; i < count; ++i) {
-        const T cur = next;
-        if (i + 1 < count)
-            next = x[static_cast<long long>(i + 1) * stride];
-        r = cr_hypot<T>(r, cur);
-    }
-    return r;
-}
-
-// The nonzero elements of x[0..count) (stride apart) copied in order to out[0..nz); returns nz.
-// A correctly rounded hypot with a zero operand returns the other operand's magnitude exactly,
-// and every partial result of a norm chain is already nonnegative, so a chain over the nonzero
-// elements alone gives the same bits as the chain over all of them. The reduced matrices of the
-// SPAI fits are sparse (a stencil column's fit touches 7 of ~50 shadow rows before fill-in), so
-// this removes about 40 % of the chain steps, the sequential part of every fit.
-template <class Grp, class T>
-__device__ int grp_compact_nonzero(const Grp &g, const T *x, int count, long long stride, T *out) {
-    const int lane = g.thread_rank();
-    constexpr int GS = Grp::size();
-    int nz = 0;
-    for (int t0 = 0; t0 < count; t0 += GS) {
-        const int t = t0 + lane;
-        T val = T(0);
-        if (t < count)
-            val = x[t * stride];
-        const bool keep = val != T(0);
-        const unsigned bal = g.ballot(keep);
-        if (keep)
-            out[nz + __popc(bal & ((1u << lane) - 1u))] = val;
-        nz += __popc(bal);
-    }
-    g.sync();
-    return nz;
+    NormChain<T> st;
+    for (int i = 0; i < count; ++i)
+        norm_chain_step(st, x[static_cast<long long>(i) * stride]);
+    return st.c;
 }
 
 template <bool FAST, class Grp, class T>
 __device__ int grp_least_squares(const Grp &g, T *R, T *rhs, int m, int q, T *coef, T *v,
-                                 T &pivot_ratio, PhaseClock *clk = nullptr, T *scratch = nullptr) {
+                                 T &pivot_ratio, PhaseClock *clk = nullptr) {
     const int lane = g.thread_rank();
     constexpr int GS = Grp::size();
     if (m < q)
@@ -419,21 +393,9 @@ __device__ int grp_least_squares(const Grp &g, T *R, T *rhs, int m, int q, T *co
         if (FAST) {
             length = grp_norm(g, R + static_cast<long long>(j) * q + j, m - j, q);
         } else {
-            // chain over the column's nonzeros (compacted into v, which is rewritten below)
-            const int nz = grp_compact_nonzero(g, R + static_cast<long long>(j) * q + j, m - j, q, v);
-            if (lane == 0) {
-                if (clk && clk->out) {
-                    // tuning aid: how many groups' chains the warp runs together (lanes active here)
-                    const unsigned am = __activemask();
-                    if (static_cast<int>(threadIdx.x & 31) == __ffs(am) - 1) {
-                        atomicAdd(clk->out + kPhCount, static_cast<unsigned long long>(__popc(am)));
-                        atomicAdd(clk->out + kPhCount + 1, 1ull);
-                    }
-                }
-                length = norm_chain(v, nz, 1);
-            }
+            if (lane == 0)
+                length = norm_chain(R + static_cast<long long>(j) * q + j, m - j, q);
             length = g.shfl(length, 0);
-            g.sync();
         }
         if (!isfinite(length))
             return kNumericalFailure;
@@ -451,12 +413,10 @@ __device__ int grp_least_squares(const Grp &g, T *R, T *rhs, int m, int q, T *co
                 v[0] += copysign(T(1), v[0]);
             vnorm = sqrt(T(2) * (T(1) + fabs(x0) / length));
         } else {
-            if (lane == 0)
+            if (lane == 0) {
                 v[0] += copysign(T(1), v[0]);
-            g.sync();
-            const int nz = grp_compact_nonzero(g, v, m - j, 1, scratch);
-            if (lane == 0)
-                vnorm = norm_chain(scratch, nz, 1);
+                vnorm = norm_chain(v, m - j, 1);
+            }
             vnorm = g.shfl(vnorm, 0);
         }
         g.sync();
@@ -628,7 +588,7 @@ __device__ int fit_column(const Grp &g, const ColumnArgs<T> &A, int k, char *ws,
         g.sync();
         T pivot_ratio = 0;
         clk.mark(kPhQr); // gather
-        const int ls = grp_least_squares<FAST>(g, R, rhs, m, q, coef, v, pivot_ratio, &clk, s);
+        const int ls = grp_least_squares<FAST>(g, R, rhs, m, q, coef, v, pivot_ratio, &clk);
         clk.mark(kPhQr);
         if (ls != kSuccess) {
             status = ls;
@@ -654,9 +614,8 @@ __device__ int fit_column(const Grp &g, const ColumnArgs<T> &A, int k, char *ws,
         if (FAST) {
             res = grp_norm(g, s, m, 1);
         } else {
-            const int nz = grp_compact_nonzero(g, s, m, 1, v); // v is free after the fit
             if (lane == 0)
-                res = norm_chain(v, nz, 1);
+                res = norm_chain(s, m, 1);
             res = g.shfl(res, 0);
         }
         clk.mark(kPhResidual);
@@ -1151,6 +1110,104 @@ inline std::vector<TierPlan> plan_tiers(size_t first_ws, int first_G, int max_th
     return tiers;
 }
 
+// First-tier choice of the autotuner and its timings on the sample.
+struct TuneChoice {
+    int G = 0;          // 0: not tuned
+    size_t ws = 0;
+    double ms = 0, default_ms = 0;
+};
+
+// Autotuner for the SPAI's first workspace tier (lanes per column group, workspace bytes per
+// group). Which pair is fastest depends on the sparsity profile: the workspace bounds how many
+// groups stay resident, a column whose fit outgrows it is refitted from the start in the next
+// tier, and wider groups shorten the parallel phases of a fit but leave more lanes idle in its
+// sequential norm chains. The tuner runs the whole tier chain on an evenly spaced column sample
+// for each candidate pair of the profile (the default first), times it with CUDA events and
+// keeps the fastest; the choice is cached per profile (value type, size, row-length profile and
+// the construction parameters) for the life of the process. Fits are deterministic, so the
+// choice changes the speed of construction only, never its result. Samples: 49,152 columns for
+// short rows, 8,192 for heavy-tailed rows (their fits cost about 200 times more), a quarter of
+// the columns at most; matrices with fewer than 16,384 columns keep the default.
+template <class T, class RunChain>
+TuneChoice tune_first_tier(const DeviceCsr<T> &a, const SpaiParams &prm, bool heavy, int G_def, size_t ws_def,
+                           int max_threads, size_t smem_budget, int sms, cudaStream_t st, ColumnArgs<T> args,
+                           int *queue, int *err, unsigned long long *top, bool verbose, RunChain &run_chain) {
+    (void)sms;
+    const int n = a.n;
+    const int S = std::min(heavy ? 8192 : 49152, n / 4);
+    if (S < 4096)
+        return TuneChoice{};
+    using Key = std::tuple<int, int, int, int, int, double, long long, int>;
+    static std::mutex mu;
+    static std::map<Key, TuneChoice> cache;
+    const Key key{static_cast<int>(sizeof(T)), prm.fast ? 1 : 0, n, a.nnz, a.max_row, prm.epsilon, prm.alpha,
+                  prm.beta};
+    {
+        std::lock_guard<std::mutex> lock(mu);
+        const auto it = cache.find(key);
+        if (it != cache.end())
+            return it->second;
+    }
+    std::vector<std::pair<int, size_t>> cands;
+    if (heavy)
+        cands = {{G_def, ws_def}, {32, 28672}, {16, 14336}, {32, 57344}, {8, 14336}};
+    else if (sizeof(T) == 4)
+        cands = {{G_def, ws_def}, {8, 4096}, {8, 3072}, {4, 3072}, {8, 6144}, {16, 10240}};
+    else
+        cands = {{G_def, ws_def}, {8, 10240}, {8, 8192}, {4, 8192}, {16, 12288}};
+    args.phase = nullptr;
+    DeviceArena mem; // sample list and global workspaces of the sample runs (freed on return)
+    int *list = mem.alloc<int>(S);
+    std::vector<int> h(S);
+    for (int i = 0; i < S; ++i)
+        h[i] = static_cast<int>(static_cast<long long>(i) * n / S);
+    SPAI_CUDA(cudaMemcpyAsync(list, h.data(), sizeof(int) * S, cudaMemcpyHostToDevice, st));
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    SPAI_CUDA(cudaEventCreate(&e0));
+    SPAI_CUDA(cudaEventCreate(&e1));
+    TuneChoice best;
+    double best_ms = INFINITY;
+    for (size_t c = 0; c < cands.size(); ++c) {
+        const int G = cands[c].first;
+        const size_t ws = cands[c].second;
+        if (ws > smem_budget || G * 4 > max_threads)
+            continue;
+        const std::vector<TierPlan> tiers = plan_tiers(ws, G, max_threads, smem_budget, 0);
+        SPAI_CUDA(cudaMemsetAsync(queue, 0, sizeof(int) * 64, st));
+        SPAI_CUDA(cudaMemcpyAsync(&queue[62], &S, sizeof(int), cudaMemcpyHostToDevice, st));
+        SPAI_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
+        SPAI_CUDA(cudaMemsetAsync(top, 0, sizeof(unsigned long long), st));
+        SPAI_CUDA(cudaEventRecord(e0, st));
+        int m0 = 0, gc = 0;
+        run_chain(tiers, args, list, S, mem, false, m0, gc);
+        SPAI_CUDA(cudaEventRecord(e1, st));
+        SPAI_CUDA(cudaEventSynchronize(e1));
+        float ms = 0;
+        SPAI_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        if (verbose)
+            std::fprintf(stderr, "spai tune: G=%d ws=%zu sample=%d  %.2f ms (first-tier misfits %d)\n", G, ws, S, ms, m0);
+        if (c == 0)
+            best.default_ms = ms;
+        if (ms < best_ms) {
+            best_ms = ms;
+            best.G = G;
+            best.ws = ws;
+            best.ms = ms;
+        }
+    }
+    SPAI_CUDA(cudaEventDestroy(e0));
+    SPAI_CUDA(cudaEventDestroy(e1));
+    // The sample runs wrote per-column outputs and packed entries: the full run rewrites every
+    // column, and the counters start again from zero.
+    SPAI_CUDA(cudaMemsetAsync(queue, 0, sizeof(int) * 64, st));
+    SPAI_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
+    SPAI_CUDA(cudaMemsetAsync(top, 0, sizeof(unsigned long long), st));
+    SPAI_CUDA(cudaStreamSynchronize(st));
+    std::lock_guard<std::mutex> lock(mu);
+    cache[key] = best;
+    return best;
+}
+
 template <class T>
 void SpaiBuilder<T>::construct(const DeviceCsr<T> &a, const SpaiParams &prm, cudaStream_t st,
                                SpaiOutput<T> &out, DeviceArena &arena) {
@@ -1208,22 +1265,22 @@ void SpaiBuilder<T>::construct(const DeviceCsr<T> &a, const SpaiParams &prm, cud
     unsigned long long cap = std::max<unsigned long long>(static_cast<unsigned long long>(n) * 24ull, 1ull << 16);
     int *pidx = nullptr;
     T *pv = nullptr;
-    // Autotuned defaults from the sparsity profile (row lengths bound the shadow and candidate
-    // sets): short-row matrices (stencils) use many small workspaces; heavy-tailed rows use
-    // fewer, larger ones. Overrides come from SpaiParams.
+    // First workspace tier: an explicit override, else the autotuner's choice for this sparsity
+    // profile (timed on a column sample, see tune_first_tier), else the profile default: short-row
+    // matrices (stencils) use many small workspaces, heavy-tailed rows fewer, larger ones.
     const bool heavy = a.max_row > 48 || static_cast<double>(nnz) > 12.0 * n;
-    const int G0 = prm.group_lanes > 0 ? prm.group_lanes : (heavy ? 16 : 8);
-    const int ws_default = heavy ? 28672 : (sizeof(T) == 8 ? 12288 : 5120);
-    const size_t ws0 = prm.ws_bytes_per_warp > 0 ? prm.ws_bytes_per_warp : ws_default;
+    const int G_def = heavy ? 16 : 8;
+    const size_t ws_def = heavy ? 28672 : (sizeof(T) == 8 ? 12288 : 5120);
+    int G0 = prm.group_lanes > 0 ? prm.group_lanes : G_def;
+    size_t ws0 = prm.ws_bytes_per_warp > 0 ? static_cast<size_t>(prm.ws_bytes_per_warp) : ws_def;
     const size_t smem_budget = 225 * 1024;
     // Threads per block within the register budget of one block (124 registers/thread for
     // binary64, 77 for binary32 -> at most 512 / 768 threads).
     const int max_threads = sizeof(T) == 8 ? 512 : 768;
     if (ws0 > smem_budget)
         throw ArgumentError("SPAI workspace per group too large for one block's shared memory");
-    const std::vector<TierPlan> tiers = plan_tiers(ws0, G0, max_threads, smem_budget, prm.first_qcap);
-    out.group_lanes = tiers[0].G;
-    out.ws_bytes = static_cast<int>(tiers[0].ws);
+    out.tuned = false;
+    out.tune_sample_ms = out.tune_default_ms = 0;
     int sms = 0, dev = 0;
     SPAI_CUDA(cudaGetDevice(&dev));
     SPAI_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
@@ -1232,32 +1289,23 @@ void SpaiBuilder<T>::construct(const DeviceCsr<T> &a, const SpaiParams &prm, cud
     auto clock_ms = [] {
         return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
     };
-    for (int attempt = 0;; ++attempt) {
-        pidx = arena.alloc<int>(cap);
-        pv = arena.alloc<T>(cap);
-        SPAI_CUDA(cudaMemsetAsync(queue, 0, sizeof(int) * 64, st));
-        SPAI_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
-        SPAI_CUDA(cudaMemsetAsync(top, 0, sizeof(unsigned long long), st));
-        unsigned long long *phase = nullptr;
-        if (trace) {
-            phase = arena.alloc<unsigned long long>(kPhCount + 2);
-            SPAI_CUDA(cudaMemsetAsync(phase, 0, sizeof(unsigned long long) * (kPhCount + 2), st));
-        }
-        ColumnArgs<T> args{n, a.rp, a.ci, a.val, tp, ti, d, static_cast<T>(prm.epsilon), prm.alpha,
-                           prm.beta, out.col_status, out.col_fits, out.col_growths, out.col_clamps,
-                           out.col_q, out.col_residual, off, pidx, pv, top, cap, err, phase, heavy ? 1 : 0};
-        out.overflow_columns = 0;
-        out.overflow_columns_global = 0;
-        int pending = n;          // columns the next tier takes
-        const int *in_list = nullptr;
+    // Runs a tier chain over a column list (in_list == nullptr: every column; otherwise `count`
+    // columns listed in device memory, their count at queue[62]). Global-memory workspaces come
+    // from ws_arena. Returns the misfits of the first tier and the columns that reached a global
+    // tier.
+    auto run_chain = [&](const std::vector<TierPlan> &tiers, ColumnArgs<T> args, const int *in_list, int count,
+                         DeviceArena &ws_arena, bool verbose, int &misfits0, int &global_cols) {
+        misfits0 = 0;
+        global_cols = 0;
+        int pending = count;
         int *lists[2] = {ovl, ovl2};
         for (size_t ti_ = 0; ti_ < tiers.size() && pending > 0; ++ti_) {
             const TierPlan &tp_ = tiers[ti_];
             const bool last = ti_ + 1 == tiers.size();
             int *out_list = last ? nullptr : lists[ti_ & 1];
-            TierIo io{in_list, ti_ == 0 ? nullptr : &queue[2 * ti_ - 1], &queue[2 * ti_], out_list,
-                      &queue[2 * ti_ + 1]};
-            const double t0 = trace ? clock_ms() : 0.0;
+            TierIo io{in_list, ti_ == 0 ? (in_list ? &queue[62] : nullptr) : &queue[2 * ti_ - 1], &queue[2 * ti_],
+                      out_list, &queue[2 * ti_ + 1]};
+            const double t0 = verbose ? clock_ms() : 0.0;
             const int threads = ((tp_.groups_per_block * tp_.G + 31) / 32) * 32;
             char *gws = nullptr;
             long long blocks = (static_cast<long long>(pending) + tp_.groups_per_block - 1) / tp_.groups_per_block;
@@ -1265,9 +1313,9 @@ void SpaiBuilder<T>::construct(const DeviceCsr<T> &a, const SpaiParams &prm, cud
                 const long long groups = std::min<long long>(pending, ti_ + 2 == tiers.size() ? sms * 24LL : 512LL);
                 blocks = (groups + tp_.groups_per_block - 1) / tp_.groups_per_block;
                 // one workspace for every launched group (blocks * groups_per_block >= groups)
-                gws = arena.alloc<char>(tp_.ws * static_cast<size_t>(blocks * tp_.groups_per_block));
-                if (out.overflow_columns_global == 0)
-                    out.overflow_columns_global = pending;
+                gws = ws_arena.alloc<char>(tp_.ws * static_cast<size_t>(blocks * tp_.groups_per_block));
+                if (global_cols == 0)
+                    global_cols = pending;
             }
             launch_columns<T>(prm.fast, tp_.G, args, io, tp_.ws, tp_.qcap, gws, threads, blocks, sms, st);
             ++out.launches;
@@ -1276,28 +1324,58 @@ void SpaiBuilder<T>::construct(const DeviceCsr<T> &a, const SpaiParams &prm, cud
                 SPAI_CUDA(cudaMemcpyAsync(&h_next, &queue[2 * ti_ + 1], sizeof(int), cudaMemcpyDeviceToHost, st));
             }
             SPAI_CUDA(cudaStreamSynchronize(st));
-            if (trace)
+            if (verbose)
                 std::fprintf(stderr, "spai tier %zu: G=%d ws=%zu%s groups/block=%d columns=%d  %.1f ms, misfits %d\n", ti_,
                              tp_.G, tp_.ws, tp_.global ? " (global)" : "", tp_.groups_per_block, pending,
                              clock_ms() - t0, h_next);
             if (ti_ == 0)
-                out.overflow_columns = h_next;
+                misfits0 = h_next;
             pending = h_next;
             in_list = out_list;
         }
+    };
+    const bool want_tune = prm.tune && prm.group_lanes <= 0 && prm.ws_bytes_per_warp <= 0 && prm.first_qcap <= 0;
+    for (int attempt = 0;; ++attempt) {
+        pidx = arena.alloc<int>(cap);
+        pv = arena.alloc<T>(cap);
+        SPAI_CUDA(cudaMemsetAsync(queue, 0, sizeof(int) * 64, st));
+        SPAI_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
+        SPAI_CUDA(cudaMemsetAsync(top, 0, sizeof(unsigned long long), st));
+        unsigned long long *phase = nullptr;
+        if (trace) {
+            phase = arena.alloc<unsigned long long>(kPhCount);
+            SPAI_CUDA(cudaMemsetAsync(phase, 0, sizeof(unsigned long long) * kPhCount, st));
+        }
+        ColumnArgs<T> args{n, a.rp, a.ci, a.val, tp, ti, d, static_cast<T>(prm.epsilon), prm.alpha,
+                           prm.beta, out.col_status, out.col_fits, out.col_growths, out.col_clamps,
+                           out.col_q, out.col_residual, off, pidx, pv, top, cap, err, phase, heavy ? 1 : 0};
+        if (attempt == 0 && want_tune) {
+            const TuneChoice c = tune_first_tier<T>(a, prm, heavy, G_def, ws_def, max_threads, smem_budget, sms, st,
+                                                    args, queue, err, top, trace, run_chain);
+            if (c.G > 0) {
+                G0 = c.G;
+                ws0 = c.ws;
+                out.tuned = true;
+                out.tune_sample_ms = c.ms;
+                out.tune_default_ms = c.default_ms;
+            }
+        }
+        const std::vector<TierPlan> tiers = plan_tiers(ws0, G0, max_threads, smem_budget, prm.first_qcap);
+        out.group_lanes = tiers[0].G;
+        out.ws_bytes = static_cast<int>(tiers[0].ws);
+        run_chain(tiers, args, nullptr, n, arena, trace, out.overflow_columns, out.overflow_columns_global);
         if (trace && phase) {
-            unsigned long long hp[kPhCount + 2];
+            unsigned long long hp[kPhCount];
             SPAI_CUDA(cudaMemcpy(hp, phase, sizeof(hp), cudaMemcpyDeviceToHost));
             double tot = 0;
-            for (int i = 0; i < kPhCount; ++i)
-                tot += static_cast<double>(hp[i]);
+            for (unsigned long long v : hp)
+                tot += static_cast<double>(v);
             static const char *names[kPhCount] = {"shadow", "qr_other", "residual", "candidates",
                                                   "scores", "select", "qr_norms", "qr_update"};
             std::fprintf(stderr, "spai fit phases (lane-0 cycles, all tiers):");
             for (int i = 0; i < kPhCount; ++i)
                 std::fprintf(stderr, " %s %.1f%%", names[i], tot > 0 ? 100.0 * hp[i] / tot : 0.0);
-            std::fprintf(stderr, "; column-length chains per warp issue %.2f\n",
-                         hp[kPhCount + 1] ? static_cast<double>(hp[kPhCount]) / hp[kPhCount + 1] : 0.0);
+            std::fprintf(stderr, "\n");
         }
         int h_err = 0;
         SPAI_CUDA(cudaMemcpyAsync(&h_err, err, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -1387,14 +1465,21 @@ template void score_kat<float>(float, float, float, double *);
 namespace spai {
 __global__ void hypot_eval_kernel(int precision, long long count, const double *a, const double *b, double *out) {
     for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < count;
-         i += static_cast<long long>(gridDim.x) * blockDim.x)
-        out[i] = precision == 0 ? cr_hypot<double>(a[i], b[i])
-                                : static_cast<double>(cr_hypot<float>(static_cast<float>(a[i]), static_cast<float>(b[i])));
+         i += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const float af = static_cast<float>(a[i]), bf = static_cast<float>(b[i]);
+        switch (precision) {
+        case 0: out[i] = cr_hypot<double>(a[i], b[i]); break;
+        case 1: out[i] = static_cast<double>(cr_hypot<float>(af, bf)); break;
+        case 2: out[i] = norm_chain_step_from<double>(fabs(a[i]), b[i]); break;
+        default: out[i] = static_cast<double>(norm_chain_step_from<float>(fabsf(af), bf)); break;
+        }
+    }
 }
 } // namespace spai
 
-// The device hypot on host arrays (precision 0: binary64; otherwise binary32 on the operands
-// rounded to binary32, returned widened). Check hook for the SPAI norm chains.
+// The device hypot on host arrays (precision 0: binary64; 1: binary32 on the operands rounded to
+// binary32, returned widened; 2 / 3: the binary64 / binary32 norm-chain step from the running
+// norm |a|, which must return the same bits as 0 / 1). Check hook for the SPAI norm chains.
 extern "C" int spai_hypot_device(int32_t precision, int64_t count, const double *a, const double *b, double *out) {
     if (count < 0 || (count > 0 && (!a || !b || !out)))
         return spai_api_fail(-1, "spai_hypot_device: bad arguments");

@@ -75,6 +75,7 @@ struct SpaiParams {
     bool fast = false;           // parallel norms/mean, hashed candidates (not bit-reproducing)
     size_t overflow_ws_bytes = 0;
     int first_qcap = 0;          // pattern capacity of the first workspace tier; 0 = by size
+    bool tune = true;            // time first-tier candidates on a column sample (large n)
 };
 
 template <class T> struct SpaiOutput {
@@ -85,6 +86,8 @@ template <class T> struct SpaiOutput {
     int overflow_columns = 0;
     long long launches = 0;
     int group_lanes = 0, ws_bytes = 0;
+    bool tuned = false;                             // first tier chosen by the autotuner
+    double tune_sample_ms = 0, tune_default_ms = 0; // chosen / default pair's time on the sample
     int overflow_columns_global = 0;
     T *d = nullptr;
     int *col_status = nullptr, *col_fits = nullptr, *col_growths = nullptr, *col_clamps = nullptr,

@@ -132,6 +132,7 @@ SIGNATURES = {
     "spai_profile": (ctypes.c_int, [VP, ctypes.c_int32]),
     "spai_profile_read": (ctypes.c_int, [VP, ctypes.c_int32, F64P, I64P, F64P]),
     "spai_backward_error_noalloc": (ctypes.c_int, [VP, VP, VP, VP, VP]),
+    "spai_tuning": (ctypes.c_int, [VP, I32P, F64P]),
     "spai_hypot_device": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int64, F64P, F64P, F64P]),
     "spai_hypot": (ctypes.c_double, [ctypes.c_double, ctypes.c_double]),
     "spai_hypotf": (ctypes.c_float, [ctypes.c_float, ctypes.c_float]),
@@ -280,6 +281,15 @@ class Handle:
         """Allocation-free backward error of device vector x (see spai_backward_error_noalloc)."""
         _check(lib().spai_backward_error_noalloc(self._h, VP(d_b), VP(d_x), VP(d_out), stream))
 
+    def tuning(self):
+        """Autotuner choices of the last build / solve set-up (see spai_tuning)."""
+        out = np.zeros(5, np.int32)
+        ms = np.zeros(2)
+        _check(lib().spai_tuning(self._h, _p(out, I32P), _p(ms, F64P)))
+        return dict(group_lanes=int(out[0]), ws_bytes=int(out[1]), spai_tuned=bool(out[2]),
+                    sell_order_a=int(out[3]), sell_order_p=int(out[4]),
+                    sample_ms=float(ms[0]), default_sample_ms=float(ms[1]))
+
     def history(self):
         """History of the last solve run with FLAG_HISTORY: (outer, inner, iterations) record lists."""
         no, ni, nt = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
@@ -373,12 +383,16 @@ def mm_read(path, device_min_lines=0):
         lib().spai_mm_free(h)
 
 
+HYPOT_KINDS = {"f64": 0, "f32": 1, "f64-chain": 2, "f32-chain": 3}
+
+
 def hypot_device(a, b, precision="f64"):
-    """The device hypot on arrays (binary32 for precision "f32": operands rounded, result widened)."""
+    """The device hypot on arrays (binary32 for "f32": operands rounded, result widened);
+    "f64-chain" / "f32-chain": the SPAI norm-chain step with |a| as the running norm."""
     a = np.ascontiguousarray(a, np.float64)
     b = np.ascontiguousarray(b, np.float64)
     out = np.zeros(len(a))
-    _check(lib().spai_hypot_device(0 if precision == "f64" else 1, len(a), _p(a, F64P), _p(b, F64P), _p(out, F64P)))
+    _check(lib().spai_hypot_device(HYPOT_KINDS[precision], len(a), _p(a, F64P), _p(b, F64P), _p(out, F64P)))
     return out
 
 

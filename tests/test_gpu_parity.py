@@ -292,8 +292,16 @@ def _hypot_cases_f32(rng, count):
     y = np.sqrt(mid * mid - x.astype(np.float64) ** 2).astype(np.float32)
     yu = np.nextafter(y, np.float32(np.inf))
     trip = np.array([3, 4, 5, 8, 15, 17, 20, 21, 29], np.float32)
-    return (np.concatenate([a, x, x, trip[:4]]).astype(np.float64),
-            np.concatenate([b, y, yu, trip[4:8]]).astype(np.float64))
+    # Zeros, subnormals, infinities, the edges of the norm-chain step's direct range (2^-40, 2^40)
+    # and of its negligible-operand rule (ratio 2^-14).
+    edge = np.array([0.0, 1.0, 2.0 ** -149, 2.0 ** -130, 2.0 ** -126, 2.0 ** -41, 2.0 ** -40, 2.0 ** -39,
+                     2.0 ** 39, 2.0 ** 40, 2.0 ** 41, 2.0 ** 100, 3.0e38, np.inf], np.float32)
+    ea, eb = np.meshgrid(edge, edge)
+    ratio = np.array([1.0, 1.5, 1.999])
+    ra = np.concatenate([ratio, ratio, ratio]).astype(np.float32)
+    rb = np.concatenate([ratio * 2.0 ** -14, ratio * 2.0 ** -13, ratio * 2.0 ** -15]).astype(np.float32)
+    return (np.concatenate([a, x, x, trip[:4], ea.ravel(), ra]).astype(np.float64),
+            np.concatenate([b, y, yu, trip[4:8], eb.ravel(), rb]).astype(np.float64))
 
 
 def _hypot_cases_f64(rng, count):
@@ -312,15 +320,25 @@ def _hypot_cases_f64(rng, count):
         x = float(mid * Decimal(float(f)))
         ys.append(float((mid * mid - Decimal(x) * Decimal(x)).sqrt()))
         xs.append(x)
-    return np.concatenate([a, xs]), np.concatenate([b, ys])
+    edge = np.array([0.0, 1.0, 5e-324, 2.0 ** -1030, 2.0 ** -1022, 2.0 ** -401, 2.0 ** -400, 2.0 ** -399,
+                     2.0 ** 399, 2.0 ** 400, 2.0 ** 401, 1e300, 1.7e308, np.inf])
+    ea, eb = np.meshgrid(edge, edge)
+    ratio = np.array([1.0, 1.5, 1.999])
+    ra = np.concatenate([ratio, ratio, ratio])
+    rb = np.concatenate([ratio * 2.0 ** -30, ratio * 2.0 ** -29, ratio * 2.0 ** -31])
+    return np.concatenate([a, xs, ea.ravel(), ra]), np.concatenate([b, ys, eb.ravel(), rb])
 
 
-@pytest.mark.parametrize("prec", ["f32", "f64"])
+@pytest.mark.parametrize("prec", ["f32", "f64", "f32-chain", "f64-chain"])
 def test_device_hypot_matches_oracle(built, prec):
+    """The device's correctly rounded hypot, and the norm-chain step of the SPAI fits (which
+    carries the running norm's exact square), bit for bit against the oracle's hypot, including
+    operands whose exact hypot lies next to a rounding midpoint."""
     rng = np.random.default_rng(77)
-    a, b = (_hypot_cases_f32 if prec == "f32" else _hypot_cases_f64)(rng, 200000)
+    f32 = prec.startswith("f32")
+    a, b = (_hypot_cases_f32 if f32 else _hypot_cases_f64)(rng, 200000)
     got = spai_ir.hypot_device(a, b, prec)
-    ref = O.hypotf if prec == "f32" else O.hypot
+    ref = O.hypotf if f32 else O.hypot
     want = np.array([ref(float(u), float(v)) for u, v in zip(a, b)])
     bad = np.flatnonzero(got != want)
     assert bad.size == 0, [(a[i], b[i], got[i], want[i]) for i in bad[:5]]
@@ -423,3 +441,43 @@ def test_long_gmres_chunked_passes(built, prec, cap, tol):
     xo, ro = O.gmres(system, p, rhs, tol=1e-30, cap=cap, precision="f64" if prec == "f64" else "f32")
     assert ro["iterations"] == cap
     assert np.linalg.norm(x - xo) <= tol * np.linalg.norm(xo), np.linalg.norm(x - xo) / np.linalg.norm(xo)
+
+
+# ---------------------------------------------------------------------------------------------
+# Lagged second Gram-Schmidt projection (two basis reads per Arnoldi step) against the three-pass
+# form: the same statuses and refinement steps, Arnoldi counts within one step per GMRES solve,
+# the backward-error target met, and the oracle's solution.
+# ---------------------------------------------------------------------------------------------
+@pytest.mark.parametrize("prec,grid", [("mixed", 24), ("f64", 24)])
+def test_lagged_gram_schmidt_matches_three_pass(built, monkeypatch, prec, grid):
+    system = M.convection_diffusion_3d(grid)
+    n = system[0]
+    b = M.equal_rhs(n)
+    tol = 1e-12
+    opts = spai_ir.cli_options(n, prec, innercap=200, be_tolerance=tol)
+    res = {}
+    for lag in ("1", "0"):
+        monkeypatch.setenv("SPAI_CGS_LAG", lag)
+        with spai_ir.Handle(system, prec) as h:
+            h.build(opts)
+            h.profile(True)
+            x, rep = h.solve(b, opts)
+            prof = h.profile_read()
+            rng = np.random.default_rng(3)
+            rhs = rng.standard_normal(n)
+            tau = 1e-8 if prec == "f64" else 1e-4
+            xg, rg = h.gmres(rhs, tau)
+        res[lag] = (x, rep, prof, rg)
+    (xl, rl, pl, gl), (x3, r3, p3, g3) = res["1"], res["0"]
+    # the lagged run really skipped the third pass, the three-pass run really ran it
+    assert pl["cgs_pass3"]["launches"] == 0 and pl["cgs_pass2"]["launches"] > 0
+    assert p3["cgs_pass3"]["launches"] > 0
+    assert rl["converged"] and r3["converged"]
+    assert rl["ir_status"] == r3["ir_status"] and rl["outer_steps"] == r3["outer_steps"]
+    assert abs(rl["inner_iterations"] - r3["inner_iterations"]) <= rl["inner_attempts"]
+    assert rl["backward_error"] <= tol
+    assert gl["status"] == g3["status"] == 0 and abs(gl["iterations"] - g3["iterations"]) <= 1
+    assert gl["final_relative"] <= tau
+    xo, ro = O.ir(system, b, precision=prec, innercap=200, be_tolerance=tol)
+    assert ro["converged"]
+    assert np.max(np.abs(xl - xo)) <= 1e-10 * np.max(np.abs(xo))
