@@ -304,12 +304,30 @@ def run_ours(args, rank, world, local):
                 "classes": {k: {"ms": round(v["ms"], 3), "GB/s": round(v["bytes"] / (v["ms"] * 1e-3) / 1e9, 1)
                                 if v["ms"] > 0 else 0.0} for k, v in prof.items()}}
     p_mixed = handles["mixed"].preconditioner()
+    tuning = handles["mixed"].tuning()
     for hh in handles.values():
         hh.close()
     return {"system": system, "eps": eps, "desc": desc, "data": data,
             "p": p_mixed, "ms": ms_mixed, "rb": rb_m, "rs": rs_m, "launches": launches, "e2e": e2e, "h2d": h2d,
             "d2h": d2h, "fp64": fp64, "roofline": roofline, "clocks": clocks.summary(), "n": n,
-            "nnz": len(val)}
+            "nnz": len(val), "tuning": tuning}
+
+
+def spai_kernel_line(res):
+    """The SPAI construction kernel is bound by the latency of its sequential correctly rounded
+    norm chains, not by HBM (its DRAM throughput is a fraction of a percent): report columns and
+    fits per second, the autotuner's first-tier choice and the pipe utilisation measured by ncu
+    (profiles/spai_util.json, written from a capture of the same kernel on a smaller grid)."""
+    ms = res["rb"]["spai_ms"]
+    line = {"kernel": "spai_columns_kernel", "bound": "latency (sequential hypot chains)", "ms": round(ms, 2),
+            "columns_per_s": round(res["n"] / (ms * 1e-3)), "fits_per_s": round(res["rb"]["spai_fits"] / (ms * 1e-3)),
+            "fits": res["rb"]["spai_fits"], "tuning": res.get("tuning")}
+    try:
+        with open(os.path.join(ROOT, "profiles", "spai_util.json")) as f:
+            line["ncu"] = json.load(f)
+    except Exception:
+        pass
+    return line
 
 
 def run_batched(steps=2, warmup=1):
@@ -474,6 +492,7 @@ def main():
                 "d2h_bytes_per_step": res["d2h"]},
         "gpu_launches": int(res["launches"]),
         "roofline": res["roofline"],
+        "spai_kernel": spai_kernel_line(res),
         "cpu_baseline": cpu,
         "clocks": res["clocks"],
         "solve": {"spai_ms": round(res["rb"]["spai_ms"], 2), "refine_ms": round(res["rs"]["solve_ms"], 2),

@@ -285,8 +285,9 @@ int spai_profile_read(spai_handle *h, int32_t cls, double *ms, int64_t *launches
  * src/cuda_spai.cu:575-577). out[0] lanes per column group and out[1] workspace bytes per group
  * of the SPAI's first workspace tier; out[2] = 1 when the autotuner chose them (first-tier
  * candidates timed on a column sample, cached per sparsity profile for the process), 0 for the
- * profile default or an override; out[3] / out[4] slice order of the Krylov SpMV with the inner
- * A / with P (0 natural rows, 1 rows sorted by length, -1 no solve set up yet).
+ * profile default or an override; out[3] / out[4] layout of the Krylov SpMV with the inner A /
+ * with P (0 sliced ELLPACK over natural rows, 1 over rows sorted by length, 2 one array per
+ * occupied diagonal; -1 no solve set up yet).
  * ms (optional, 2 doubles): the chosen pair's and the default pair's time on the sample (NaN
  * when not tuned). Returns SPAI_OK or an error code. */
 int spai_tuning(spai_handle *h, int32_t *out, double *ms);

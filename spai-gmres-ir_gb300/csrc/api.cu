@@ -987,8 +987,8 @@ int spai_tuning(spai_handle *h, int32_t *out, double *ms) {
     int oa = -1, op = -1;
     auto orders = [&](const auto &e) {
         if (e.n > 0) {
-            oa = e.sa.sorted() ? 1 : 0;
-            op = e.sp.sorted() ? 1 : 0;
+            oa = e.sa.layout;
+            op = e.sp.layout;
         }
     };
     if (h->engine_cap >= 0) {

@@ -15,23 +15,20 @@
 // applies the Givens rotations and sets the acceptance flags, exactly as the single-pass
 // version did. Reductions are deterministic (fixed tile assignment, fixed trees).
 //
-// Lagged second projection (MODE 4 and 5; two basis reads per step instead of three, used while
-// every step streams whole tiles). After the second dots h2 = V^T w' of step k the new vector
-// is left stored as w' = W_{k+1}, with h2 kept as its pending correction c and with
-// h(k+1,k) = ||w''|| = sqrt(||w'||^2 - ||h2||^2) (the second projection removes an orthogonal
-// component). Step k+1 then works with the uncorrected vector and fixes the algebra instead:
-//   z = P A s_{k+1} W_{k+1} = P A v_{k+1} + V E,  E = s_{k+1} H_u c  (H_u the unrotated
-//       Hessenberg: P A V_k = V_{k+1} H_u), so every projection is the computed one minus E;
-//   pass 4: D_j = W_j^T z (as stored), d_j = s_j D_j for j <= k, d_{k+1} -= s_{k+1} c^T d,
-//           h1 = d - E, ||P A v_{k+1}||^2 = ||z||^2 - 2 E^T d + ||E||^2;
-//   pass 5: per tile, W_{k+1} -= sum_j c_j s_j W_j (the correction, written back), then
-//           w' = z - sum_j d_j v_j (E cancels in the orthogonalised vector; the correction of
-//           W_{k+1} is folded into the coefficients, so both combinations read each segment of
-//           the stage once), second dots with the corrected segments, ||w'||.
-// The DGKS test, the Hessenberg column h1 [+ h2], the Givens rotations and the acceptance
-// flags are those of the three-pass version; only the order in which the correction reaches
-// memory changes. The solution only ever combines corrected vectors (W_0..W_k after pass 5 of
-// step k).
+// Lagged second projection (MODE 4 and 5: two basis reads per step instead of three, used while
+// every step streams whole tiles). The second projection h2 = V^T w' of a step is never applied
+// to memory: the new vector is stored as w' = S_{k+1} with h(k+1,k) = ||w''|| =
+// sqrt(||w'||^2 - ||h2||^2), and the true basis is V = S U^-1 with U upper triangular
+// (U[j][k+1] = h2_j, U[k+1][k+1] = h(k+1,k)); its inverse Ui grows by one column per step
+// (Ui[:, k+1] = (-Ui h2 / h(k+1,k), 1 / h(k+1,k))). With z = P A S_{k+1} / h(k+1,k) =
+// P A v_{k+1} + V E, E = H_u h2 / h(k+1,k) (H_u the unrotated Hessenberg: P A V_k = V_{k+1} H_u):
+//   pass 4: D = S^T z and ||z|| (a pass 1 over the stored vectors); d = Ui^T D, h1 = d - E,
+//           ||P A v_{k+1}||^2 = ||z||^2 - 2 E^T d + ||E||^2, update coefficients f = Ui d;
+//   pass 5: w' = z - S f (= z - V d: E cancels in the orthogonalised vector), second dots
+//           E2 = S^T w', ||w'|| (a pass 2 with coefficients f); h2 = Ui^T E2, the DGKS decision,
+//           the Hessenberg column h1 [+ h2], the next Ui column and E, the Givens update.
+// The DGKS test, Hessenberg column, Givens rotations and acceptance flags are those of the
+// three-pass form; the candidate combines the stored vectors with coefficients Ui y.
 //
 // Streaming: while k + 1 segments fit in a pipeline stage, each block streams its tiles through
 // two shared-memory stages filled by asynchronous 16-byte copies (cp.async, one commit group per
@@ -109,9 +106,10 @@ template <class T> struct CgsArgs {
     int stage_segs;     // segments per pipeline stage (at least 2)
     T *gacc;            // large caps: per-block dot accumulators and coefficients in global memory
     T *gcf;             //   ([gridDim][cap + 2] each); nullptr: both in shared memory
-    // Lagged second projection (MODE 4 / 5): projections d of the current step, the pending
-    // correction c of the newest vector, its Hessenberg image E and the unrotated Hessenberg.
-    T *dl, *cpend, *ecorr, *Hu;
+    // Lagged second projection (MODE 4 / 5): true projections d, update coefficients f on the
+    // stored vectors, the correction image E, the unrotated Hessenberg H_u and the inverse Ui of
+    // the basis' triangular factor (both column-major with leading dimension hld).
+    T *dl, *fco, *ecorr, *Hu, *Ui;
 };
 
 constexpr int kCgsStages = 2;
@@ -119,11 +117,11 @@ constexpr int kCgsWarps = kCgsThreads / 32;
 
 // Dynamic shared memory of a pass: accumulators, coefficients and per-warp accumulators first,
 // then the staging region (kCgsStages stages of stage_segs segments).
-// Accumulators and the two coefficient arrays ([cap + 2] each) live in shared memory up to this
-// size, in per-block global scratch beyond it (very long GMRES caps). Per-warp accumulators hold
-// half a stage (stage_segs / 2 + 1 entries) each: the streamed path needs them only when several
-// tiles share a stage (k + 2 <= stage_segs / 2), and one tile per stage writes each dot straight
-// to its single owner; the chunked path keeps them while k + 1 fits.
+// Accumulators and coefficients ([cap + 2] each) live in shared memory up to this size, in
+// per-block global scratch beyond it (very long GMRES caps). Per-warp accumulators hold half a
+// stage (stage_segs / 2 + 1 entries) each: the streamed path needs them only when several tiles
+// share a stage (k + 2 <= stage_segs / 2), one tile per stage writing each dot straight to its
+// single owner; the chunked path keeps them while k + 1 fits.
 constexpr size_t kCgsSharedAccMax = 64 * 1024;
 template <class T> __host__ __device__ inline bool cgs_acc_global(int cap) {
     return 2 * static_cast<size_t>(cap + 2) * sizeof(T) > kCgsSharedAccMax;
@@ -132,14 +130,14 @@ __host__ __device__ inline int cgs_warp_slots(int stage_segs) {
     return stage_segs / 2 + 1;
 }
 template <class T> __host__ __device__ inline size_t cgs_region_offset(int cap, int stage_segs) {
-    const size_t accs = cgs_acc_global<T>(cap) ? 0 : 3 * static_cast<size_t>(cap + 2);
+    const size_t accs = cgs_acc_global<T>(cap) ? 0 : 2 * static_cast<size_t>(cap + 2);
     return ((accs + static_cast<size_t>(kCgsWarps) * cgs_warp_slots(stage_segs)) * sizeof(T) + 127) &
            ~static_cast<size_t>(127);
 }
 // Largest stage (in 512-byte segments) that fits beside the accumulators; a tile at step k needs
 // k + 2 segments (basis and source), so cap + 1 covers every step.
 template <class T> inline int cgs_stage_segs(int cap, size_t dyn_budget) {
-    const size_t fixed = ((cgs_acc_global<T>(cap) ? 0 : 3) * static_cast<size_t>(cap + 2) +
+    const size_t fixed = ((cgs_acc_global<T>(cap) ? 0 : 2) * static_cast<size_t>(cap + 2) +
                           static_cast<size_t>(kCgsWarps)) * sizeof(T) + 256;
     if (fixed >= dyn_budget)
         return 0;
@@ -289,8 +287,8 @@ template <class T> __device__ void finish_column(Ctl *ctl, T *H, int hld, T *cs,
 template <class T, int MODE>
 __global__ void __launch_bounds__(kCgsThreads) cgs_pass_kernel(CgsArgs<T> a) {
     constexpr int R = TileGeom<T>::R;
-    // The lagged passes stream like passes 1 (dots) and 2 (update and second dots).
-    constexpr bool LAGA = MODE == 4, LAGB = MODE == 5;
+    // The lagged passes stream exactly like passes 1 (dots) and 2 (update and second dots).
+    constexpr bool LAGA = MODE == 4, LAGB = MODE == 5, LAG = LAGA || LAGB;
     constexpr int BM = LAGA ? 1 : (LAGB ? 2 : MODE);
     Ctl *ctl = a.ctl;
     if (!ctl->active)
@@ -303,33 +301,20 @@ __global__ void __launch_bounds__(kCgsThreads) cgs_pass_kernel(CgsArgs<T> a) {
                   : reinterpret_cast<T *>(dyn);                     // [cap + 2] dot accumulators
     T *cf = gacc ? a.gcf + static_cast<size_t>(blockIdx.x) * (ctl->cap + 2)
                  : acc + (ctl->cap + 2);                            // [cap + 2] update coefficients h_j s_j
-    T *cc = gacc ? nullptr : cf + (ctl->cap + 2);                   // [cap + 2] lagged correction c_j s_j
     T *accw = gacc ? reinterpret_cast<T *>(dyn)
-                   : cc + (ctl->cap + 2);                           // [warps][stage_segs / 2 + 1]
+                   : cf + (ctl->cap + 2);                           // [warps][stage_segs / 2 + 1]
     T *region = reinterpret_cast<T *>(dyn + cgs_region_offset<T>(ctl->cap, a.stage_segs)); // staging (128-byte aligned)
     __shared__ T red[kCgsThreads / 32];
     const int k = ctl->k;
     const int kk = k + 1; // segments 0..k
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const T *coef = BM == 2 ? a.h1 : a.h2; // h_j (coefficient h_j s_j applied below)
-    // Lagged update: W_k carries the pending correction c (when the last step reorthogonalised);
-    // w' = z - sum_{j<k} s_j (d_j - d_k s_k c_j) W_j - d_k s_k W_k, and W_k -= sum_{j<k} c_j s_j W_j.
-    const bool pend = LAGB && ctl->lag_pending && !gacc;
     for (int j = threadIdx.x; j < kk; j += blockDim.x) {
         acc[j] = 0;
-        if (LAGB) {
-            const T dks = a.dl[k] * a.V.scale[k];
-            if (j < k) {
-                const T cj = pend ? a.cpend[j] : T(0);
-                cf[j] = a.V.scale[j] * (a.dl[j] - dks * cj);
-                if (cc)
-                    cc[j] = cj * a.V.scale[j];
-            } else {
-                cf[j] = dks;
-            }
-        } else if (BM >= 2) {
+        if (LAGB)
+            cf[j] = a.fco[j]; // f = Ui d: coefficients on the stored vectors
+        else if (BM >= 2)
             cf[j] = coef[j] * a.V.scale[j];
-        }
     }
     // Per-thread power-of-two scaled sum of squares of the current vector (no block syncs):
     // value = ts * 2^(2 te); rescaling by powers of two is exact.
@@ -355,7 +340,7 @@ __global__ void __launch_bounds__(kCgsThreads) cgs_pass_kernel(CgsArgs<T> a) {
     const bool streamed = tseg <= a.stage_segs;
     // Partial updates of the warps (passes 2 and 3), shared by the streamed and chunked paths.
     __shared__ __align__(16) typename Vec16<T>::V wpart_all[BM >= 2 ? kCgsWarps : 1][32];
-    if ((LAGA || LAGB) && !streamed) {
+    if (LAG && !streamed) {
         // The engine runs the lagged passes only when every step of the solve streams.
         if (blockIdx.x == 0 && threadIdx.x == 0) {
             ctl->status = 8;
@@ -433,12 +418,7 @@ __global__ void __launch_bounds__(kCgsThreads) cgs_pass_kernel(CgsArgs<T> a) {
         // Pass 2 keeps a warp's segments in registers between the update and the second dot
         // products when it owns few enough of them (one shared-memory read of the tile, not two).
         constexpr int kCache = sizeof(T) == 4 ? 12 : 6;
-        const bool cache = MODE == 2 && (kk + P - 1) / P <= kCache;
-        // Lagged update (pass 5): with a pending correction and P > 1 warps per tile, the first
-        // hc = P / 2 warps of a tile sum the correction sum_{j<k} c_j s_j W_j (segments
-        // j = part mod hc) and the others the update (j = part - hc mod P - hc), so both
-        // combinations fit the one partial-update array; one warp per tile computes both.
-        const int hc = P / 2;
+        const bool cache = BM == 2 && (kk + P - 1) / P <= kCache;
         V16 vr[kCache];
         auto update_part = [&](const T *tile) {
             V16 acc4 = VT::zero();
@@ -463,38 +443,7 @@ __global__ void __launch_bounds__(kCgsThreads) cgs_pass_kernel(CgsArgs<T> a) {
             }
             return acc4;
         };
-        auto lag_parts = [&](const T *tile, V16 &up4, V16 &co4) {
-            up4 = VT::zero();
-            co4 = VT::zero();
-            if (P == 1) {
-#pragma unroll 4
-                for (int j = 0; j < kk; ++j) {
-                    const V16 sg = *reinterpret_cast<const V16 *>(tile + j * R + lane * E);
-                    up4 = VT::axpy(cf[j], sg, up4);
-                    if (pend && j < k)
-                        co4 = VT::axpy(cc[j], sg, co4);
-                }
-            } else if (!pend) {
-#pragma unroll 4
-                for (int j = part; j < kk; j += P)
-                    up4 = VT::axpy(cf[j], *reinterpret_cast<const V16 *>(tile + j * R + lane * E), up4);
-            } else if (part < hc) {
-#pragma unroll 4
-                for (int j = part; j < k; j += hc)
-                    co4 = VT::axpy(cc[j], *reinterpret_cast<const V16 *>(tile + j * R + lane * E), co4);
-            } else {
-#pragma unroll 4
-                for (int j = part - hc; j < kk; j += P - hc)
-                    up4 = VT::axpy(cf[j], *reinterpret_cast<const V16 *>(tile + j * R + lane * E), up4);
-            }
-        };
-        // Segment j of the tile for the dots; the lagged pass uses the corrected W_k (wk).
-        auto seg_at = [&](const T *tile, int j, const V16 &wk) {
-            if (LAGB && j == k)
-                return wk;
-            return *reinterpret_cast<const V16 *>(tile + j * R + lane * E);
-        };
-        auto dots = [&](const T *tile, V16 cur, V16 wk) {
+        auto dots = [&](const T *tile, V16 cur) {
             if (cache) {
 #pragma unroll
                 for (int i = 0; i < kCache; ++i) {
@@ -511,13 +460,13 @@ __global__ void __launch_bounds__(kCgsThreads) cgs_pass_kernel(CgsArgs<T> a) {
                     for (int u = 0; u < 8; ++u) {
                         const int j = part + (i0 + u) * P;
                         if (j < kk)
-                            racc[i0 + u] += VT::dot(seg_at(tile, j, wk), cur);
+                            racc[i0 + u] += VT::dot(*reinterpret_cast<const V16 *>(tile + j * R + lane * E), cur);
                     }
                 }
             } else {
 #pragma unroll 2
                 for (int j = part; j < kk; j += P) {
-                    T d = VT::dot(seg_at(tile, j, wk), cur);
+                    T d = VT::dot(*reinterpret_cast<const V16 *>(tile + j * R + lane * E), cur);
                     for (int o = 16; o > 0; o >>= 1)
                         d += __shfl_xor_sync(0xffffffffu, d, o);
                     if (lane == 0)
@@ -547,28 +496,17 @@ __global__ void __launch_bounds__(kCgsThreads) cgs_pass_kernel(CgsArgs<T> a) {
                 const int t = static_cast<int>(blockIdx.x) + (q0 + qq) * static_cast<int>(gridDim.x);
                 const T *tile = sbase + static_cast<size_t>(qq) * tseg * R;
                 V16 cur = *reinterpret_cast<const V16 *>(tile + kk * R + lane * E);
-                V16 wk = VT::zero();
                 if (BM >= 2) {
-                    V16 acc4, co4 = VT::zero();
-                    if (LAGB)
-                        lag_parts(tile, acc4, co4);
-                    else
-                        acc4 = update_part(tile);
+                    const V16 acc4 = update_part(tile);
                     if (P > 1) {
-                        // combined after the block barrier below
-                        wpart[warp][lane] = (pend && part < hc) ? co4 : acc4;
+                        wpart[warp][lane] = acc4; // combined after the block barrier below
                         break;
-                    }
-                    if (LAGB) {
-                        wk = VT::sub(*reinterpret_cast<const V16 *>(tile + k * R + lane * E), co4);
-                        if (pend)
-                            *reinterpret_cast<V16 *>(a.V.seg(t, k) + lane * E) = wk; // corrected W_k
                     }
                     cur = VT::sub(cur, acc4); // pad rows: every operand is zero there
                     *reinterpret_cast<V16 *>(a.V.seg(t, kk) + lane * E) = cur; // W_{k+1}
                 }
                 if (BM <= 2)
-                    dots(tile, cur, wk);
+                    dots(tile, cur);
                 if (part == 0)
                     for (int e = 0; e < E; ++e) {
                         const T v = VT::get(cur, e);
@@ -587,19 +525,9 @@ __global__ void __launch_bounds__(kCgsThreads) cgs_pass_kernel(CgsArgs<T> a) {
                     const int qq = slot;
                     const int t = static_cast<int>(blockIdx.x) + (q0 + qq) * static_cast<int>(gridDim.x);
                     const T *tile = sbase + static_cast<size_t>(qq) * tseg * R;
-                    const int p0 = pend ? hc : 0; // lagged with a correction: partials [0, hc) correct W_k
-                    V16 tot = wpart[slot * P + p0][lane];
-                    for (int p2 = p0 + 1; p2 < P; ++p2)
+                    V16 tot = wpart[slot * P][lane];
+                    for (int p2 = 1; p2 < P; ++p2)
                         tot = VT::add(tot, wpart[slot * P + p2][lane]);
-                    V16 wk = VT::zero();
-                    if (LAGB) {
-                        V16 co = VT::zero();
-                        for (int p2 = 0; p2 < p0; ++p2)
-                            co = VT::add(co, wpart[slot * P + p2][lane]);
-                        wk = VT::sub(*reinterpret_cast<const V16 *>(tile + k * R + lane * E), co);
-                        if (pend && part == 0)
-                            *reinterpret_cast<V16 *>(a.V.seg(t, k) + lane * E) = wk; // corrected W_k
-                    }
                     V16 cur = VT::sub(*reinterpret_cast<const V16 *>(tile + kk * R + lane * E), tot);
                     if (part == 0) {
                         *reinterpret_cast<V16 *>(a.V.seg(t, kk) + lane * E) = cur; // W_{k+1}
@@ -614,7 +542,7 @@ __global__ void __launch_bounds__(kCgsThreads) cgs_pass_kernel(CgsArgs<T> a) {
                         }
                     }
                     if (BM == 2)
-                        dots(tile, cur, wk);
+                        dots(tile, cur);
                 }
             }
             __syncthreads(); // the slot is free
@@ -840,7 +768,8 @@ __global__ void __launch_bounds__(kCgsThreads) cgs_pass_kernel(CgsArgs<T> a) {
     __threadfence();
     const int nb = gridDim.x;
     // Dots: one warp per j, lanes over blocks, fixed tree.
-    T *hout = LAGA ? a.dl : (BM == 1 ? a.h1 : a.h2);
+    // The lagged passes keep the raw dots S^T z (in acc, reused) for the triangular transform.
+    T *hout = LAG ? acc : (BM == 1 ? a.h1 : a.h2);
     if (BM <= 2)
         for (int j = warp; j < kk; j += nw) {
             T sdot = 0;
@@ -849,7 +778,7 @@ __global__ void __launch_bounds__(kCgsThreads) cgs_pass_kernel(CgsArgs<T> a) {
             for (int o = 16; o > 0; o >>= 1)
                 sdot += __shfl_xor_sync(0xffffffffu, sdot, o);
             if (lane == 0)
-                hout[j] = sdot * a.V.scale[j]; // h_j = s_j W_j^T w
+                hout[j] = LAG ? sdot : sdot * a.V.scale[j]; // h_j = s_j W_j^T w
         }
     // Norm: parallel max of exponents, then rescaled sum (fixed tree).
     __shared__ int emax_sh;
@@ -875,31 +804,43 @@ __global__ void __launch_bounds__(kCgsThreads) cgs_pass_kernel(CgsArgs<T> a) {
                 part_s += ldexp(norms[b].s, 2 * (norms[b].e - E));
     const T S = block_sum(part_s, red);
     __syncthreads();
-    if (LAGA || LAGB) {
+    if (LAG) {
+        // Raw dots S^T z (pass 4) or S^T w' (pass 5) are in acc[0..k].
         const T nrm = nb_bad ? T(NAN) : (E == INT_MIN ? T(0) : ldexp(sqrt(S), E));
+        const long long ld = a.hld;
         if (LAGA) {
-            // d_k = s_k W_k^T z - s_k c^T d, h1 = d - E, ||P A v_k||^2 = ||z||^2 - 2 E^T d + ||E||^2.
-            if (warp == 0) {
-                const bool pa = ctl->lag_pending != 0;
-                T cd = 0;
-                if (pa)
-                    for (int j = lane; j < k; j += 32)
-                        cd += a.cpend[j] * a.dl[j];
+            if (k == 0 && threadIdx.x == 0)
+                a.Ui[0] = a.V.scale[0]; // S_0 = W_0 is a true basis vector: U = (1 / s_0)
+            __syncthreads();
+            const bool pa = ctl->lag_pending != 0;
+            // d = Ui^T D (warp per entry, lanes down column j of Ui), h1 = d - E.
+            for (int j = warp; j <= k; j += nw) {
+                T t = 0;
+                for (int i = lane; i <= j; i += 32)
+                    t += a.Ui[i + j * ld] * acc[i];
                 for (int o = 16; o > 0; o >>= 1)
-                    cd += __shfl_xor_sync(0xffffffffu, cd, o);
-                const T dk = a.dl[k] - a.V.scale[k] * cd;
-                __syncwarp();
-                if (lane == 0)
-                    a.dl[k] = dk;
-                __syncwarp();
-                T ed = 0, ee = 0;
-                for (int j = lane; j <= k; j += 32) {
-                    const T e = pa ? a.ecorr[j] : T(0);
-                    const T dj = a.dl[j];
-                    a.h1[j] = dj - e;
-                    ed += e * dj;
-                    ee += e * e;
+                    t += __shfl_xor_sync(0xffffffffu, t, o);
+                if (lane == 0) {
+                    a.dl[j] = t;
+                    a.h1[j] = t - (pa ? a.ecorr[j] : T(0));
                 }
+            }
+            __syncthreads();
+            // f = Ui d (thread per entry, columns in order: coalesced across the threads).
+            for (int i = threadIdx.x; i <= k; i += blockDim.x) {
+                T f = 0;
+                for (int j = i; j <= k; ++j)
+                    f += a.Ui[i + j * ld] * a.dl[j];
+                a.fco[i] = f;
+            }
+            if (warp == 0) {
+                T ed = 0, ee = 0;
+                if (pa)
+                    for (int j = lane; j <= k; j += 32) {
+                        const T e = a.ecorr[j];
+                        ed += e * a.dl[j];
+                        ee += e * e;
+                    }
                 for (int o = 16; o > 0; o >>= 1) {
                     ed += __shfl_xor_sync(0xffffffffu, ed, o);
                     ee += __shfl_xor_sync(0xffffffffu, ee, o);
@@ -909,10 +850,19 @@ __global__ void __launch_bounds__(kCgsThreads) cgs_pass_kernel(CgsArgs<T> a) {
             }
             return;
         }
-        // LAGB: DGKS test; with a second projection the new vector keeps h2 as its pending
-        // correction and h(k+1,k) = sqrt(||w'||^2 - ||h2||^2). Then the Hessenberg column (rotated
-        // copy H and unrotated H_u), the correction image E = s_{k+1} H_u c for the next step,
-        // and the Givens update.
+        // Pass 5: h2 = Ui^T E2.
+        for (int j = warp; j <= k; j += nw) {
+            T t = 0;
+            for (int i = lane; i <= j; i += 32)
+                t += a.Ui[i + j * ld] * acc[i];
+            for (int o = 16; o > 0; o >>= 1)
+                t += __shfl_xor_sync(0xffffffffu, t, o);
+            if (lane == 0)
+                a.h2[j] = t;
+        }
+        __syncthreads();
+        // DGKS test; with a second projection, h(k+1,k) = sqrt(||w'||^2 - ||h2||^2) and h2 stays
+        // the pending correction of the new stored vector.
         __shared__ T lag_sh[2];
         if (warp == 0) {
             T hh = 0;
@@ -921,9 +871,8 @@ __global__ void __launch_bounds__(kCgsThreads) cgs_pass_kernel(CgsArgs<T> a) {
             for (int o = 16; o > 0; o >>= 1)
                 hh += __shfl_xor_sync(0xffffffffu, hh, o);
             if (lane == 0) {
-                const bool finite = isfinite(nrm);
-                const bool ro = finite && (a.always_reorth ||
-                                           !(nrm >= T(0.70710678118654752) * static_cast<T>(ctl->wnorm)));
+                const bool ro = isfinite(nrm) && (a.always_reorth ||
+                                                 !(nrm >= T(0.70710678118654752) * static_cast<T>(ctl->wnorm)));
                 lag_sh[0] = ro ? T(1) : T(0);
                 lag_sh[1] = ro ? sqrt(fmax(nrm * nrm - hh, T(0))) : nrm;
             }
@@ -931,25 +880,29 @@ __global__ void __launch_bounds__(kCgsThreads) cgs_pass_kernel(CgsArgs<T> a) {
         __syncthreads();
         const bool ro = lag_sh[0] != T(0);
         const T beta = lag_sh[1];
-        T *colh = a.H + static_cast<long long>(k) * a.hld;
-        T *colu = a.Hu + static_cast<long long>(k) * a.hld;
+        const T sb = beta == T(0) ? T(0) : T(1) / beta; // s_{k+1}, as finish_column sets it
+        T *colh = a.H + k * ld;
+        T *colu = a.Hu + k * ld;
         for (int j = threadIdx.x; j <= k; j += blockDim.x) {
             const T hj = a.h1[j] + (ro ? a.h2[j] : T(0));
             colh[j] = hj;
             colu[j] = hj;
-            a.cpend[j] = ro ? a.h2[j] : T(0);
         }
         if (threadIdx.x == 0)
             colu[k + 1] = beta;
         __syncthreads();
-        if (ro) {
-            const T sb = beta == T(0) ? T(0) : T(1) / beta;
-            for (int i = threadIdx.x; i <= k + 1; i += blockDim.x) {
-                T e = 0;
+        // Next column of Ui: (-Ui h2 / h(k+1,k), 1 / h(k+1,k)); E = H_u h2 / h(k+1,k).
+        T *uin = a.Ui + (k + 1) * ld;
+        for (int i = threadIdx.x; i <= k + 1; i += blockDim.x) {
+            T u = 0, e = 0;
+            if (ro) {
+                for (int j = i; j <= k; ++j)
+                    u += a.Ui[i + j * ld] * a.h2[j];
                 for (int j = max(i - 1, 0); j <= k; ++j)
-                    e += a.cpend[j] * a.Hu[i + static_cast<long long>(j) * a.hld];
-                a.ecorr[i] = e * sb;
+                    e += a.Hu[i + j * ld] * a.h2[j];
             }
+            uin[i] = i == k + 1 ? sb : -u * sb;
+            a.ecorr[i] = e * sb;
         }
         if (threadIdx.x != 0)
             return;
@@ -1028,9 +981,10 @@ __global__ void __launch_bounds__(256) spmv_basis_kernel(int n, const int *__res
     }
 }
 
-// x = sum_{j < count} (y_j s_j) W_j (candidate correction; x0 = 0).
+// x = sum_{j < count} (y_j s_j) W_j (candidate correction; x0 = 0); unit != 0: y holds the
+// coefficients on the stored vectors (lagged Gram-Schmidt), x = sum_j y_j W_j.
 template <class T>
-__global__ void __launch_bounds__(256) form_candidate_tiles_kernel(int n, Basis<T> V, const T *y,
+__global__ void __launch_bounds__(256) form_candidate_tiles_kernel(int n, Basis<T> V, const T *y, int unit,
                                                                    T *x, const Ctl *ctl) {
     constexpr int R = TileGeom<T>::R;
     if (!ctl->active || !ctl->vgate)
@@ -1041,7 +995,7 @@ __global__ void __launch_bounds__(256) form_candidate_tiles_kernel(int n, Basis<
         T acc = 0;
 #pragma unroll 8
         for (int j = 0; j < count; ++j)
-            acc += (y[j] * V.scale[j]) * p[static_cast<long long>(j) * R];
+            acc += (unit ? y[j] : y[j] * V.scale[j]) * p[static_cast<long long>(j) * R];
         x[i] = acc;
     }
 }

@@ -22,6 +22,7 @@
 #include "krylov.cuh"
 #include "cgs_tiles.cuh"
 #include "sell.cuh"
+#include "dia.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -213,7 +214,8 @@ __global__ void __launch_bounds__(kBlock) norm_kernel(int n, VecRef<T> ar, const
 // at every step once the recursive estimate has dropped below tau on systems whose recomputed
 // residual stays above it.
 template <class T>
-__global__ void __launch_bounds__(256) solve_y_kernel(Ctl *ctl, const T *H, int hld, const T *g, T *y) {
+__global__ void __launch_bounds__(256) solve_y_kernel(Ctl *ctl, const T *H, int hld, const T *g, T *y,
+                                                      const T *Ui = nullptr, T *yc = nullptr) {
     if (!ctl->active || !ctl->vgate)
         return;
     const int k = ctl->k;
@@ -251,6 +253,14 @@ __global__ void __launch_bounds__(256) solve_y_kernel(Ctl *ctl, const T *H, int 
         __syncthreads();
     }
     bad = __syncthreads_or(bad);
+    // Lagged Gram-Schmidt: the candidate combines the stored vectors, V y = S (Ui y).
+    if (Ui && !bad)
+        for (int i = threadIdx.x; i < count; i += blockDim.x) {
+            T c = 0;
+            for (int j = i; j < count; ++j)
+                c += Ui[i + static_cast<long long>(j) * hld] * y[j];
+            yc[i] = c;
+        }
     if (threadIdx.x == 0) {
         ctl->formed = count;
         if (bad) {
@@ -758,6 +768,117 @@ DeviceSell<T> tuned_sell(DeviceArena &arena, const DeviceCsr<T> &m, int sms, cud
     return t_srt < t_nat ? srt : nat;
 }
 
+// Diagonal-layout SpMVs (stencil-like profiles, dia.cuh).
+template <class T>
+__global__ void __launch_bounds__(kBlock) dia_spmv_kernel(DeviceDia<T> m, VecRef<T> x, VecRef<T> y, const int *gate) {
+    if (gate && !*gate)
+        return;
+    const T *xv = x.get();
+    dia_rows(m, [&](int c) { return __ldg(xv + c); }, T(1), y.get());
+}
+template <class T>
+__global__ void __launch_bounds__(kBlock) dia_spmv_basis_kernel(DeviceDia<T> m, Basis<T> V, T *y, const Ctl *ctl) {
+    constexpr int R = TileGeom<T>::R;
+    if (!ctl->active)
+        return;
+    const int k = ctl->k;
+    const T *base = V.base + static_cast<long long>(k) * R;
+    const long long tstride = static_cast<long long>(V.cap1) * R;
+    dia_rows(m, [&](int c) { return base[(c / R) * tstride + (c % R)]; }, V.scale[k], y);
+}
+
+// A Krylov SpMV operand in the layout the tuner chose: sliced ELLPACK (natural or length-sorted
+// rows) or diagonals.
+template <class T> struct KrylovOp {
+    DeviceSell<T> sell;
+    DeviceDia<T> dia;
+    int layout = 0; // 0 sliced, natural rows; 1 sliced, rows sorted by length; 2 diagonals
+    // Algorithmic bytes of one SpMV: stored entries (+ indices) and row data, x and y once.
+    double bytes(int n, long long nnz) const {
+        if (layout == 2)
+            return static_cast<double>(dia.ndiag) * n * sizeof(T) + 4.0 * n + 2.0 * n * sizeof(T);
+        return static_cast<double>(nnz) * (4 + sizeof(T)) + 4.0 * (n + 1) + 2.0 * n * sizeof(T);
+    }
+};
+template <class T>
+void launch_op(const KrylovOp<T> &op, VecRef<T> x, VecRef<T> y, const int *gate, int sms, cudaStream_t st) {
+    if (op.layout == 2) {
+        dia_spmv_kernel<T><<<grid_for(op.dia.n, kBlock, sms * 8), kBlock, 0, st>>>(op.dia, x, y, gate);
+        SPAI_LAUNCH("dia_spmv_kernel");
+        return;
+    }
+    launch_sell<T>(op.sell, x, y, gate, sms, st);
+}
+template <class T> void launch_op_basis(const KrylovOp<T> &op, Basis<T> V, T *y, const Ctl *ctl, int sms, cudaStream_t st) {
+    if (op.layout == 2) {
+        dia_spmv_basis_kernel<T><<<grid_for(op.dia.n, kBlock, sms * 8), kBlock, 0, st>>>(op.dia, V, y, ctl);
+        SPAI_LAUNCH("dia_spmv_basis_kernel");
+        return;
+    }
+    const unsigned blocks = grid_for(static_cast<long long>(op.sell.nslices) * 32, kBlock, sms * 8);
+    sell_spmv_basis_kernel<T><<<blocks, kBlock, 0, st>>>(op.sell, V, y, ctl);
+    SPAI_LAUNCH("sell_spmv_basis_kernel");
+}
+
+// Autotuned layout of a Krylov SpMV operand: the slice order (tuned_sell), then, for profiles
+// with at most kDiaMax column offsets whose diagonals move fewer bytes than the slices, the
+// diagonal layout, timed against the sliced one on one SpMV each (best of three) and kept when
+// faster. Every layout sums each row in CSR order (bit-identical results). layout: -1 tune;
+// 0 / 1 / 2 force natural slices / sorted slices / diagonals (when the matrix allows them).
+// probe / pctl: time the basis-gather kernel (the Arnoldi step's first SpMV) on this basis
+// instead of the plain-vector kernel.
+template <class T>
+KrylovOp<T> tuned_op(DeviceArena &arena, const DeviceCsr<T> &m, int sms, cudaStream_t st, int layout,
+                     const Basis<T> *probe = nullptr, const Ctl *pctl = nullptr) {
+    KrylovOp<T> op;
+    op.sell = tuned_sell(arena, m, sms, st, layout == 0 || layout == 1 ? layout : -1);
+    op.layout = op.sell.sorted() ? 1 : 0;
+    if (layout == 0 || layout == 1 || m.n < 4096)
+        return op;
+    const double sell_bytes = static_cast<double>(op.sell.entries) * (4 + sizeof(T));
+    op.dia = build_dia(arena, m, sms, st, layout == 2 ? INFINITY : sell_bytes);
+    if (!op.dia.ok())
+        return op;
+    if (layout == 2) {
+        op.layout = 2;
+        return op;
+    }
+    T *x = arena.alloc<T>(m.n);
+    T *y = arena.alloc<T>(m.n);
+    fill_kernel<T><<<grid_for(m.n, kBlock, sms * 8), kBlock, 0, st>>>(m.n, x, T(1));
+    SPAI_LAUNCH("fill_kernel");
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    SPAI_CUDA(cudaEventCreate(&e0));
+    SPAI_CUDA(cudaEventCreate(&e1));
+    auto time_one = [&](int lay) {
+        KrylovOp<T> o = op;
+        o.layout = lay;
+        float best = INFINITY;
+        for (int r = 0; r < 3; ++r) {
+            SPAI_CUDA(cudaEventRecord(e0, st));
+            if (probe)
+                launch_op_basis<T>(o, *probe, y, pctl, sms, st);
+            else
+                launch_op<T>(o, VecRef<T>{x, 0, nullptr, 0}, VecRef<T>{y, 0, nullptr, 0}, nullptr, sms, st);
+            SPAI_CUDA(cudaEventRecord(e1, st));
+            SPAI_CUDA(cudaEventSynchronize(e1));
+            float ms = 0;
+            SPAI_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+            best = std::min(best, ms);
+        }
+        return best;
+    };
+    const float t_sell = time_one(op.layout), t_dia = time_one(2);
+    SPAI_CUDA(cudaEventDestroy(e0));
+    SPAI_CUDA(cudaEventDestroy(e1));
+    if (std::getenv("SPAI_TRACE"))
+        std::fprintf(stderr, "spmv tune: n=%d nnz=%d sliced (%s) %.3f ms, %d diagonals %.3f ms\n", m.n, m.nnz,
+                     op.layout ? "sorted" : "natural", t_sell, op.dia.ndiag, t_dia);
+    if (t_dia < t_sell)
+        op.layout = 2;
+    return op;
+}
+
 // Optional per-kernel-class timing: CUDA events recorded on the solve stream around each
 // launch of the Arnoldi kernels. Launch records of speculative steps past the end of a GMRES
 // solve are discarded using the solve's iteration count.
@@ -823,14 +944,14 @@ template <class T, class TO> struct IrEngine {
     const DeviceCsr<TO> *a_outer = nullptr;
     const DeviceCsr<T> *a_inner = nullptr;
     const DeviceCsr<T> *p = nullptr;
-    DeviceSell<T> sa, sp; // sliced companions of the inner matrix and of P
+    KrylovOp<T> sa, sp; // SpMV layouts of the inner matrix and of P
     Ctl *ctl = nullptr;
     T *V = nullptr, *sc = nullptr, *w = nullptr, *t = nullptr, *rhs = nullptr, *pb = nullptr, *cand = nullptr,
       *ax = nullptr, *pax = nullptr, *H = nullptr, *cs = nullptr, *sn = nullptr, *g = nullptr,
       *y = nullptr, *h1 = nullptr, *h2 = nullptr, *part = nullptr, *scal = nullptr;
     // Lagged second projection: projections, pending correction, its Hessenberg image and the
     // unrotated Hessenberg (see cgs_tiles.cuh).
-    T *dl = nullptr, *cpend = nullptr, *ecorr = nullptr, *Hu = nullptr;
+    T *dl = nullptr, *fco = nullptr, *ecorr = nullptr, *Hu = nullptr, *Ui = nullptr, *yc = nullptr;
     bool lag = false; // two basis reads per Arnoldi step (every step of the solve streams)
     TO *r = nullptr, *xn = nullptr;
     NormPart *npart = nullptr;
@@ -1010,23 +1131,38 @@ template <class T, class TO> struct IrEngine {
         nblk_vec = static_cast<int>(grid_for(n, kBlock, sms * 8));
         constexpr int R = TileGeom<T>::R;
         ntiles = (n + R - 1) / R;
-        // One block per SM: the pipeline stages take most of the shared memory (the static
-        // arrays of the pass use about 10 KiB of the 227 KiB).
-        stage_segs = cgs_stage_segs<T>(cap, 212 * 1024);
+        // One block per SM: the pipeline stages take most of the shared memory, all of it that
+        // the largest static footprint of the pass kernels (about 8 KiB) leaves.
+        {
+            int dev = 0, optin = 0;
+            SPAI_CUDA(cudaGetDevice(&dev));
+            SPAI_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+            size_t stat = 0;
+            cudaFuncAttributes fa{};
+            SPAI_CUDA(cudaFuncGetAttributes(&fa, cgs_pass_kernel<T, 1>));
+            stat = std::max(stat, fa.sharedSizeBytes);
+            SPAI_CUDA(cudaFuncGetAttributes(&fa, cgs_pass_kernel<T, 2>));
+            stat = std::max(stat, fa.sharedSizeBytes);
+            SPAI_CUDA(cudaFuncGetAttributes(&fa, cgs_pass_kernel<T, 3>));
+            stat = std::max(stat, fa.sharedSizeBytes);
+            SPAI_CUDA(cudaFuncGetAttributes(&fa, cgs_pass_kernel<T, 4>));
+            stat = std::max(stat, fa.sharedSizeBytes);
+            SPAI_CUDA(cudaFuncGetAttributes(&fa, cgs_pass_kernel<T, 5>));
+            stat = std::max(stat, fa.sharedSizeBytes);
+            const size_t budget = static_cast<size_t>(optin) > stat + 1024 ? static_cast<size_t>(optin) - stat - 256 : 0;
+            stage_segs = cgs_stage_segs<T>(cap, budget);
+        }
         if (stage_segs < 2)
             throw std::runtime_error("Gram-Schmidt staging does not fit in shared memory");
         cgs_dyn = cgs_dyn_smem<T>(cap, stage_segs);
         nblk_dots = std::min(ntiles, sms);
         ctl = arena.alloc<Ctl>(1);
         cudaStream_t setup_st = nullptr;
-        // Slice order timed per operand when the natural layout pads (tuned_sell); SPAI_SELL_ORDER=0/1
-        // forces natural/sorted rows (equivalence checks and tuning sweeps).
-        int sell_order = -1;
-        if (const char *e = std::getenv("SPAI_SELL_ORDER"))
-            sell_order = std::atoi(e);
-        sa = tuned_sell(arena, ai, sms, setup_st, sell_order);
-        sp = tuned_sell(arena, pp, sms, setup_st, sell_order);
-        SPAI_CUDA(cudaStreamSynchronize(setup_st));
+        // SpMV layout timed per operand (tuned_op); SPAI_SPMV_LAYOUT=0/1/2 forces natural slices,
+        // sorted slices or diagonals (equivalence checks and tuning sweeps).
+        int layout = -1;
+        if (const char *e = std::getenv("SPAI_SPMV_LAYOUT"))
+            layout = std::atoi(e);
         const size_t vcount = static_cast<size_t>(ntiles) * (cap + 1) * R;
         {
             size_t free_b = 0, total_b = 0;
@@ -1040,6 +1176,20 @@ template <class T, class TO> struct IrEngine {
         V = arena.alloc<T>(vcount);
         SPAI_CUDA(cudaMemset(V, 0, vcount * sizeof(T))); // pad rows of the last tile stay zero
         sc = arena.alloc<T>(cap + 2);
+        {
+            // The operand that gathers the basis vector is timed in its Arnoldi form (basis
+            // gather from this basis; the control block is rewritten at the start of a solve).
+            fill_kernel<T><<<1, 256, 0, setup_st>>>(cap + 2, sc, T(1));
+            SPAI_LAUNCH("fill_kernel");
+            Ctl hc{};
+            hc.active = 1;
+            hc.k = 0;
+            SPAI_CUDA(cudaMemcpyAsync(ctl, &hc, sizeof(Ctl), cudaMemcpyHostToDevice, setup_st));
+            const Basis<T> probe{V, cap + 1, ntiles, sc};
+            sa = tuned_op(arena, ai, sms, setup_st, layout, right ? nullptr : &probe, ctl);
+            sp = tuned_op(arena, pp, sms, setup_st, layout, right ? &probe : nullptr, ctl);
+            SPAI_CUDA(cudaStreamSynchronize(setup_st));
+        }
         cgs_dots = arena.alloc<T>(static_cast<size_t>(nblk_dots) * (cap + 2));
         cgs_gacc = cgs_gcf = nullptr;
         if (cgs_acc_global<T>(cap)) {
@@ -1079,9 +1229,11 @@ template <class T, class TO> struct IrEngine {
         h1 = arena.alloc<T>(cap + 2);
         h2 = arena.alloc<T>(cap + 2);
         dl = arena.alloc<T>(cap + 2);
-        cpend = arena.alloc<T>(cap + 2);
+        fco = arena.alloc<T>(cap + 2);
         ecorr = arena.alloc<T>(cap + 2);
+        yc = arena.alloc<T>(cap + 2);
         Hu = arena.alloc<T>(static_cast<size_t>(hld) * (cap + 1));
+        Ui = arena.alloc<T>(static_cast<size_t>(hld) * (cap + 2));
         part = arena.alloc<T>(static_cast<size_t>(std::max(nblk_dots, nblk_vec)) * (cap + 2));
         npart = arena.alloc<NormPart>(std::max(nblk_dots, nblk_vec));
         dpart = arena.alloc<DiagPart>(std::max(nblk_dots, nblk_vec));
@@ -1098,7 +1250,7 @@ template <class T, class TO> struct IrEngine {
     CgsArgs<T> cgs_args() const {
         return CgsArgs<T>{n, basis(), w, h1, h2, H, cs, sn, g, sc, hld, ctl,
                           CgsScratch{cgs_dots, cgs_norms, counters + kSlotDots}, always_reorth ? 1 : 0,
-                          stage_segs, cgs_gacc, cgs_gcf, dl, cpend, ecorr, Hu};
+                          stage_segs, cgs_gacc, cgs_gcf, dl, fco, ecorr, Hu, Ui};
     }
     size_t cgs_smem() const {
         return cgs_dyn;
@@ -1140,26 +1292,20 @@ template <class T, class TO> struct IrEngine {
         // w = P·(A v) (left) or w = A·(P v) (right): the first matrix gathers the basis vector.
         const DeviceCsr<T> &m1 = right ? *p : *a_inner;
         const DeviceCsr<T> &m2 = right ? *a_inner : *p;
-        const DeviceSell<T> &s1 = right ? sp : sa;
-        const DeviceSell<T> &s2 = right ? sa : sp;
-        timed(st, kClsSpmvA, spmv_bytes(m1), [&] {
-            const unsigned blocks = grid_for(static_cast<long long>(s1.nslices) * 32, kBlock, sms * 8);
-            sell_spmv_basis_kernel<T><<<blocks, kBlock, 0, st>>>(s1, basis(), t, ctl);
-            SPAI_LAUNCH("sell_spmv_basis_kernel");
-        });
-        timed(st, kClsSpmvP, spmv_bytes(m2), [&] {
-            launch_sell<T>(s2, fixed(t), fixed(w), &ctl->active, sms, st);
-        });
+        const KrylovOp<T> &s1 = right ? sp : sa;
+        const KrylovOp<T> &s2 = right ? sa : sp;
+        timed(st, kClsSpmvA, s1.bytes(m1.n, m1.nnz), [&] { launch_op_basis<T>(s1, basis(), t, ctl, sms, st); });
+        timed(st, kClsSpmvP, s2.bytes(m2.n, m2.nnz), [&] { launch_op<T>(s2, fixed(t), fixed(w), &ctl->active, sms, st); });
         const size_t smem = cgs_smem();
         const CgsArgs<T> args = cgs_args();
         if (lag) {
-            // Dots (reads W_0..W_k and z), then update with the pending correction of W_k (reads
-            // the same, writes W_k and W_{k+1}).
+            // Dots (reads W_0..W_k and z), then update and second dots (reads the same, writes
+            // W_{k+1}); the second projection stays implicit in the basis' triangular factor.
             timed(st, kClsDots, vec_bytes(kk + 2), [&] {
                 cgs_pass_kernel<T, 4><<<nblk_dots, kCgsThreads, smem, st>>>(args);
                 SPAI_LAUNCH("cgs_pass_kernel<4>");
             });
-            timed(st, kClsUpdate, vec_bytes(kk + 4), [&] {
+            timed(st, kClsUpdate, vec_bytes(kk + 3), [&] {
                 cgs_pass_kernel<T, 5><<<nblk_dots, kCgsThreads, smem, st>>>(args);
                 SPAI_LAUNCH("cgs_pass_kernel<5>");
             });
@@ -1197,25 +1343,28 @@ template <class T, class TO> struct IrEngine {
     }
 
     void verify_checks(cudaStream_t st) {
-        solve_y_kernel<T><<<1, 256, 0, st>>>(ctl, H, hld, g, y);
+        solve_y_kernel<T><<<1, 256, 0, st>>>(ctl, H, hld, g, y, lag ? Ui : nullptr, yc);
         SPAI_LAUNCH("solve_y_kernel");
+        // Candidate coefficients: y_j s_j on the normalised basis, or Ui y on the stored vectors.
+        const T *cy = lag ? yc : y;
+        const int unit = lag ? 1 : 0;
         const int *g2 = &ctl->vgate;
         if (right) {
             // d = P·(V y); recomputed residual ||rhs - A d|| (right preconditioning leaves the
             // residual unpreconditioned, so it is also the decision's numerator).
-            form_candidate_tiles_kernel<T><<<nblk_vec, kBlock, 0, st>>>(n, basis(), y, pax, ctl);
+            form_candidate_tiles_kernel<T><<<nblk_vec, kBlock, 0, st>>>(n, basis(), cy, unit, pax, ctl);
             SPAI_LAUNCH("form_candidate_tiles_kernel");
-            launch_sell<T>(sp, fixed(pax), fixed(cand), g2, sms, st);
-            launch_sell<T>(sa, fixed(cand), fixed(ax), g2, sms, st);
+            launch_op<T>(sp, fixed(pax), fixed(cand), g2, sms, st);
+            launch_op<T>(sa, fixed(cand), fixed(ax), g2, sms, st);
             norm(st, fixed(rhs), ax, scal + 0, kSlotNormA, g2);
             launches += 3;
             return;
         }
-        form_candidate_tiles_kernel<T><<<nblk_vec, kBlock, 0, st>>>(n, basis(), y, cand, ctl);
+        form_candidate_tiles_kernel<T><<<nblk_vec, kBlock, 0, st>>>(n, basis(), cy, unit, cand, ctl);
         SPAI_LAUNCH("form_candidate_tiles_kernel");
-        launch_sell<T>(sa, fixed(cand), fixed(ax), g2, sms, st);
+        launch_op<T>(sa, fixed(cand), fixed(ax), g2, sms, st);
         norm(st, fixed(rhs), ax, scal + 0, kSlotNormA, g2);
-        launch_sell<T>(sp, fixed(ax), fixed(pax), g2, sms, st);
+        launch_op<T>(sp, fixed(ax), fixed(pax), g2, sms, st);
         norm(st, fixed(pb), pax, scal + 1, kSlotNormB, g2);
         launches += 4;
     }
@@ -1227,7 +1376,7 @@ template <class T, class TO> struct IrEngine {
         gmres_start_kernel<T><<<1, 32, 0, st>>>(ctl, scal + 2, accept_every ? 1 : 0);
         SPAI_LAUNCH("gmres_start_kernel");
         if (!right) {
-            launch_sell<T>(sp, fixed(rhs), fixed(pb), &ctl->active, sms, st);
+            launch_op<T>(sp, fixed(rhs), fixed(pb), &ctl->active, sms, st);
             ++launches;
         }
         norm(st, fixed(const_cast<T *>(pbv())), nullptr, scal + 3, kSlotNormB, &ctl->active);

@@ -287,7 +287,7 @@ class Handle:
         ms = np.zeros(2)
         _check(lib().spai_tuning(self._h, _p(out, I32P), _p(ms, F64P)))
         return dict(group_lanes=int(out[0]), ws_bytes=int(out[1]), spai_tuned=bool(out[2]),
-                    sell_order_a=int(out[3]), sell_order_p=int(out[4]),
+                    spmv_layout_a=int(out[3]), spmv_layout_p=int(out[4]),
                     sample_ms=float(ms[0]), default_sample_ms=float(ms[1]))
 
     def history(self):

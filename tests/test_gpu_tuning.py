@@ -40,7 +40,7 @@ def test_small_systems_keep_the_default(built):
         h.build(spai_ir.cli_options(system[0], "mixed"))
         t = h.tuning()
     assert not t["spai_tuned"] and t["group_lanes"] == 8 and t["ws_bytes"] == 5120
-    assert t["sell_order_a"] == -1  # no solve set up yet
+    assert t["spmv_layout_a"] == -1  # no solve set up yet
 
 
 def test_spmv_slice_order_tuning_changes_speed_only(built, monkeypatch):
@@ -51,9 +51,9 @@ def test_spmv_slice_order_tuning_changes_speed_only(built, monkeypatch):
     res = {}
     for order in (None, "0"):
         if order is None:
-            monkeypatch.delenv("SPAI_SELL_ORDER", raising=False)
+            monkeypatch.delenv("SPAI_SPMV_LAYOUT", raising=False)
         else:
-            monkeypatch.setenv("SPAI_SELL_ORDER", order)
+            monkeypatch.setenv("SPAI_SPMV_LAYOUT", order)
         with spai_ir.Handle(system, "mixed") as h:
             h.build(opts)
             x, rep = h.solve(b, opts)
@@ -62,5 +62,5 @@ def test_spmv_slice_order_tuning_changes_speed_only(built, monkeypatch):
     assert rt["converged"] and r0["converged"]
     assert rt["inner_iterations"] == r0["inner_iterations"]
     np.testing.assert_array_equal(xt, x0)
-    assert tt["sell_order_a"] in (0, 1) and tt["sell_order_p"] in (0, 1)
-    assert t0["sell_order_a"] == 0 and t0["sell_order_p"] == 0
+    assert tt["spmv_layout_a"] in (0, 1, 2) and tt["spmv_layout_p"] in (0, 1, 2)
+    assert t0["spmv_layout_a"] == 0 and t0["spmv_layout_p"] == 0
