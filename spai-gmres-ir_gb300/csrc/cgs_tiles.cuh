@@ -231,20 +231,27 @@ template <class T> __device__ T block_max(T v, T *red) {
 
 // Givens update of Hessenberg column k (src/gmres.cpp:191-214) and the acceptance triggers.
 // Runs in one thread after the column col[0..k+1] has been written.
-template <class T> __device__ void finish_column(Ctl *ctl, T *H, int hld, T *cs, T *sn, T *g, T *s,
-                                                 T hnext, bool nonfinite) {
+// col: Hessenberg column k (any memory space); csr / snr: the previous rotations to read (a
+// shared-memory copy, or cs / sn themselves); the new rotation is written to cs[k], sn[k].
+template <class T> __device__ void finish_column_at(Ctl *ctl, T *col, const T *csr, const T *snr, T *cs, T *sn,
+                                                    T *g, T *s, T hnext, bool nonfinite) {
     const int k = ctl->k;
-    T *col = H + static_cast<long long>(k) * hld;
     col[k + 1] = hnext;
     nonfinite |= !isfinite(hnext);
     ctl->hnext = static_cast<double>(hnext);
     ctl->breakdown = hnext == T(0);
     s[k + 1] = hnext == T(0) ? T(0) : T(1) / hnext;
+    // Previous rotations down the column; the entry carried to the next rotation stays in a
+    // register (same arithmetic as rotating in place).
+    T carry = k > 0 ? col[0] : T(0);
+#pragma unroll 8
     for (int r = 0; r < k; ++r) {
-        const T up = col[r], lo = col[r + 1];
-        col[r] = cs[r] * up + sn[r] * lo;
-        col[r + 1] = -sn[r] * up + cs[r] * lo;
+        const T up = carry, lo = col[r + 1];
+        col[r] = csr[r] * up + snr[r] * lo;
+        carry = -snr[r] * up + csr[r] * lo;
     }
+    if (k > 0)
+        col[k] = carry;
     const T upper = col[k];
     const T radius = cr_hypot<T>(upper, col[k + 1]);
     ctl->iterations = k + 1;
@@ -280,6 +287,10 @@ template <class T> __device__ void finish_column(Ctl *ctl, T *H, int hld, T *cs,
     const bool trig = ctl->breakdown || est <= static_cast<T>(ctl->tol_inner) || k + 1 == ctl->cap;
     ctl->triggered = trig ? 1 : 0;
     ctl->vgate = (trig || ctl->accept_every) ? 1 : 0;
+}
+template <class T> __device__ void finish_column(Ctl *ctl, T *H, int hld, T *cs, T *sn, T *g, T *s,
+                                                 T hnext, bool nonfinite) {
+    finish_column_at(ctl, H + static_cast<long long>(ctl->k) * hld, cs, sn, cs, sn, g, s, hnext, nonfinite);
 }
 
 // One Gram-Schmidt pass (MODE 1, 2 or 3, or the lagged 4 and 5; see the file comment). Grid:
@@ -474,6 +485,11 @@ __global__ void __launch_bounds__(kCgsThreads) cgs_pass_kernel(CgsArgs<T> a) {
                 }
             }
         };
+        // With several warps per tile, passes 2 and 3 no longer read the stage after the barrier that
+        // combines their partial updates when the source segment was taken into registers and the
+        // second dots use the segments cached in registers: the next item's copies into this slot
+        // are issued right after that barrier, overlapping the combine, the stores and the dots.
+        const bool early = P > 1 && BM >= 2 && (BM == 3 || cache);
         for (int item = 0; item < nitems; ++item) {
             const int st = item % nslots;
             // all but the newest nslots - 1 commit groups complete = this item has landed
@@ -492,6 +508,7 @@ __global__ void __launch_bounds__(kCgsThreads) cgs_pass_kernel(CgsArgs<T> a) {
             const int nq = min(my_tiles, q0 + tt_per) - q0;
             // P == 1: warp takes tiles slot, slot + 8, ...; P > 1: one round, tile `slot`.
             const int qstep = P == 1 ? kCgsWarps : nq + 1;
+            V16 zsave = VT::zero(); // the tile's source segment (P > 1)
             for (int qq = slot; qq < nq; qq += qstep) {
                 const int t = static_cast<int>(blockIdx.x) + (q0 + qq) * static_cast<int>(gridDim.x);
                 const T *tile = sbase + static_cast<size_t>(qq) * tseg * R;
@@ -500,6 +517,7 @@ __global__ void __launch_bounds__(kCgsThreads) cgs_pass_kernel(CgsArgs<T> a) {
                     const V16 acc4 = update_part(tile);
                     if (P > 1) {
                         wpart[warp][lane] = acc4; // combined after the block barrier below
+                        zsave = cur;
                         break;
                     }
                     cur = VT::sub(cur, acc4); // pad rows: every operand is zero there
@@ -521,6 +539,8 @@ __global__ void __launch_bounds__(kCgsThreads) cgs_pass_kernel(CgsArgs<T> a) {
             if (P > 1 && BM >= 2) {
                 // Combine the P partial updates of each tile in warp order, then finish the tile.
                 __syncthreads();
+                if (early)
+                    issue(item + nslots);
                 if (slot < nq) {
                     const int qq = slot;
                     const int t = static_cast<int>(blockIdx.x) + (q0 + qq) * static_cast<int>(gridDim.x);
@@ -528,7 +548,7 @@ __global__ void __launch_bounds__(kCgsThreads) cgs_pass_kernel(CgsArgs<T> a) {
                     V16 tot = wpart[slot * P][lane];
                     for (int p2 = 1; p2 < P; ++p2)
                         tot = VT::add(tot, wpart[slot * P + p2][lane]);
-                    V16 cur = VT::sub(*reinterpret_cast<const V16 *>(tile + kk * R + lane * E), tot);
+                    V16 cur = VT::sub(zsave, tot);
                     if (part == 0) {
                         *reinterpret_cast<V16 *>(a.V.seg(t, kk) + lane * E) = cur; // W_{k+1}
                         for (int e = 0; e < E; ++e) {
@@ -545,8 +565,10 @@ __global__ void __launch_bounds__(kCgsThreads) cgs_pass_kernel(CgsArgs<T> a) {
                         dots(tile, cur);
                 }
             }
-            __syncthreads(); // the slot is free
-            issue(item + nslots);
+            if (!early) {
+                __syncthreads(); // the slot is free
+                issue(item + nslots);
+            }
         }
         asm volatile("cp.async.wait_group 0;\n" ::: "memory");
         if (BM <= 2 && reg_dots) {
@@ -805,32 +827,86 @@ __global__ void __launch_bounds__(kCgsThreads) cgs_pass_kernel(CgsArgs<T> a) {
     const T S = block_sum(part_s, red);
     __syncthreads();
     if (LAG) {
-        // Raw dots S^T z (pass 4) or S^T w' (pass 5) are in acc[0..k].
+        // Raw dots S^T z (pass 4) or S^T w' (pass 5) are in acc[0..k]. The O(k^2) triangular
+        // products run from shared memory: the staging region is free now, and Ui's upper
+        // triangle (then, in pass 5, H_u's upper Hessenberg part) is copied into it packed by
+        // columns (coalesced), so the products below read shared memory instead of waiting on L2
+        // loads one column at a time.
         const T nrm = nb_bad ? T(NAN) : (E == INT_MIN ? T(0) : ldexp(sqrt(S), E));
         const long long ld = a.hld;
-        if (LAGA) {
-            if (k == 0 && threadIdx.x == 0)
-                a.Ui[0] = a.V.scale[0]; // S_0 = W_0 is a true basis vector: U = (1 / s_0)
-            __syncthreads();
-            const bool pa = ctl->lag_pending != 0;
-            // d = Ui^T D (warp per entry, lanes down column j of Ui), h1 = d - E.
-            for (int j = warp; j <= k; j += nw) {
-                T t = 0;
-                for (int i = lane; i <= j; i += 32)
-                    t += a.Ui[i + j * ld] * acc[i];
-                for (int o = 16; o > 0; o >>= 1)
-                    t += __shfl_xor_sync(0xffffffffu, t, o);
-                if (lane == 0) {
-                    a.dl[j] = t;
-                    a.h1[j] = t - (pa ? a.ecorr[j] : T(0));
+        T *us = region;
+        auto tri = [](int j) { return j * (j + 1) / 2; };      // column j of Ui: rows 0..j
+        auto hes = [](int j) { return j * (j + 3) / 2; };      // column j of H_u: rows 0..j+1
+        if (LAGA && k == 0 && threadIdx.x == 0)
+            a.Ui[0] = a.V.scale[0]; // S_0 = W_0 is a true basis vector: U = (1 / s_0)
+        __syncthreads();
+        // Staging copies: every thread takes packed elements e, e + blockDim, ... (four loads in
+        // flight), so the copy is one parallel sweep instead of a column after column wait on memory
+        // (the factors were written by earlier launches on other SMs and may have left L2).
+        auto stage = [&](const T *src, int nel, auto colof, auto start) {
+            for (int e0 = threadIdx.x; e0 < nel; e0 += 4 * blockDim.x) {
+                T v[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int e = e0 + u * blockDim.x;
+                    v[u] = T(0);
+                    if (e < nel) {
+                        const int j = colof(e);
+                        v[u] = src[(e - start(j)) + static_cast<long long>(j) * ld];
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int e = e0 + u * blockDim.x;
+                    if (e < nel)
+                        us[e] = v[u];
                 }
             }
+        };
+        // column of packed element e: tri(j) <= e < tri(j + 1), resp. hes(j) <= e < hes(j + 1)
+        auto tri_col = [&](int e) {
+            int j = static_cast<int>((sqrtf(8.0f * e + 1.0f) - 1.0f) * 0.5f);
+            while (j > 0 && tri(j) > e)
+                --j;
+            while (tri(j + 1) <= e)
+                ++j;
+            return j;
+        };
+        auto hes_col = [&](int e) {
+            int j = static_cast<int>((sqrtf(8.0f * e + 9.0f) - 3.0f) * 0.5f);
+            while (j > 0 && hes(j) > e)
+                --j;
+            while (hes(j + 1) <= e)
+                ++j;
+            return j;
+        };
+        stage(a.Ui, tri(k + 1), tri_col, tri);
+        __syncthreads();
+        // x = Ui^T v for v in acc (thread per entry j, rows of column j in order).
+        auto uit = [&](int j) {
+            const T *col = us + tri(j);
+            T t = 0;
+#pragma unroll 8
+            for (int i = 0; i <= j; ++i)
+                t += col[i] * acc[i];
+            return t;
+        };
+        if (LAGA) {
+            // d = Ui^T D, h1 = d - E (d also in cf, free after the streaming loop).
+            const bool pa = ctl->lag_pending != 0;
+            for (int j = threadIdx.x; j <= k; j += blockDim.x) {
+                const T t = uit(j);
+                cf[j] = t;
+                a.dl[j] = t;
+                a.h1[j] = t - (pa ? a.ecorr[j] : T(0));
+            }
             __syncthreads();
-            // f = Ui d (thread per entry, columns in order: coalesced across the threads).
+            // f = Ui d (thread per entry i, columns j >= i in order).
             for (int i = threadIdx.x; i <= k; i += blockDim.x) {
                 T f = 0;
+#pragma unroll 8
                 for (int j = i; j <= k; ++j)
-                    f += a.Ui[i + j * ld] * a.dl[j];
+                    f += us[tri(j) + i] * cf[j];
                 a.fco[i] = f;
             }
             if (warp == 0) {
@@ -838,7 +914,7 @@ __global__ void __launch_bounds__(kCgsThreads) cgs_pass_kernel(CgsArgs<T> a) {
                 if (pa)
                     for (int j = lane; j <= k; j += 32) {
                         const T e = a.ecorr[j];
-                        ed += e * a.dl[j];
+                        ed += e * cf[j];
                         ee += e * e;
                     }
                 for (int o = 16; o > 0; o >>= 1) {
@@ -850,15 +926,11 @@ __global__ void __launch_bounds__(kCgsThreads) cgs_pass_kernel(CgsArgs<T> a) {
             }
             return;
         }
-        // Pass 5: h2 = Ui^T E2.
-        for (int j = warp; j <= k; j += nw) {
-            T t = 0;
-            for (int i = lane; i <= j; i += 32)
-                t += a.Ui[i + j * ld] * acc[i];
-            for (int o = 16; o > 0; o >>= 1)
-                t += __shfl_xor_sync(0xffffffffu, t, o);
-            if (lane == 0)
-                a.h2[j] = t;
+        // Pass 5: h2 = Ui^T E2 (kept in cf for the products below).
+        for (int j = threadIdx.x; j <= k; j += blockDim.x) {
+            const T t = uit(j);
+            cf[j] = t;
+            a.h2[j] = t;
         }
         __syncthreads();
         // DGKS test; with a second projection, h(k+1,k) = sqrt(||w'||^2 - ||h2||^2) and h2 stays
@@ -867,7 +939,7 @@ __global__ void __launch_bounds__(kCgsThreads) cgs_pass_kernel(CgsArgs<T> a) {
         if (warp == 0) {
             T hh = 0;
             for (int j = lane; j <= k; j += 32)
-                hh += a.h2[j] * a.h2[j];
+                hh += cf[j] * cf[j];
             for (int o = 16; o > 0; o >>= 1)
                 hh += __shfl_xor_sync(0xffffffffu, hh, o);
             if (lane == 0) {
@@ -883,37 +955,70 @@ __global__ void __launch_bounds__(kCgsThreads) cgs_pass_kernel(CgsArgs<T> a) {
         const T sb = beta == T(0) ? T(0) : T(1) / beta; // s_{k+1}, as finish_column sets it
         T *colh = a.H + k * ld;
         T *colu = a.Hu + k * ld;
+        // The Hessenberg column goes to H_u (global) and to a shared copy in acc (the raw dots are
+        // consumed), which the Givens update below rotates; finiteness is checked here, in parallel.
+        bool nf = false;
         for (int j = threadIdx.x; j <= k; j += blockDim.x) {
-            const T hj = a.h1[j] + (ro ? a.h2[j] : T(0));
-            colh[j] = hj;
+            const T hj = a.h1[j] + (ro ? cf[j] : T(0));
+            acc[j] = hj;
             colu[j] = hj;
+            nf |= !isfinite(hj);
         }
         if (threadIdx.x == 0)
             colu[k + 1] = beta;
-        __syncthreads();
+        nf = __syncthreads_or(nf);
         // Next column of Ui: (-Ui h2 / h(k+1,k), 1 / h(k+1,k)); E = H_u h2 / h(k+1,k).
         T *uin = a.Ui + (k + 1) * ld;
-        for (int i = threadIdx.x; i <= k + 1; i += blockDim.x) {
-            T u = 0, e = 0;
-            if (ro) {
-                for (int j = i; j <= k; ++j)
-                    u += a.Ui[i + j * ld] * a.h2[j];
-                for (int j = max(i - 1, 0); j <= k; ++j)
-                    e += a.Hu[i + j * ld] * a.h2[j];
+        T ui[2] = {T(0), T(0)}; // entries i = threadIdx.x, threadIdx.x + blockDim.x (k + 1 < 2 * blockDim.x)
+        if (ro)
+            for (int r = 0; r < 2; ++r) {
+                const int i = threadIdx.x + r * blockDim.x;
+                if (i <= k) {
+                    T u = 0;
+#pragma unroll 8
+                    for (int j = i; j <= k; ++j)
+                        u += us[tri(j) + i] * cf[j];
+                    ui[r] = u;
+                }
             }
-            uin[i] = i == k + 1 ? sb : -u * sb;
+        __syncthreads(); // Ui's copy is no longer read; H_u's new column is in memory
+        if (ro) {
+            stage(a.Hu, hes(k + 1), hes_col, hes);
+            __syncthreads();
+        }
+        for (int r = 0; r < 2; ++r) {
+            const int i = threadIdx.x + r * blockDim.x;
+            if (i > k + 1)
+                continue;
+            T e = 0;
+            if (ro) {
+#pragma unroll 8
+                for (int j = max(i - 1, 0); j <= k; ++j)
+                    e += us[hes(j) + i] * cf[j];
+            }
+            uin[i] = i == k + 1 ? sb : -ui[r] * sb;
             a.ecorr[i] = e * sb;
         }
-        if (threadIdx.x != 0)
-            return;
-        bool nonfinite = !isfinite(nrm) || !isfinite(beta);
-        for (int j = 0; j <= k; ++j)
-            nonfinite |= !isfinite(colh[j]);
-        ctl->reorth = 0;
-        ctl->lag_pending = ro ? 1 : 0;
-        if (ro)
-            ctl->reorth_count += 1;
-        finish_column(ctl, a.H, a.hld, a.cs, a.sn, a.g, a.s, beta, nonfinite);
+        // Givens update from shared copies of the column and of the previous rotations, then the
+        // rotated column to H.
+        __syncthreads(); // the staging region is free
+        T *cssh = us, *snsh = us + (k + 1);
+        for (int r = threadIdx.x; r < k; r += blockDim.x) {
+            cssh[r] = a.cs[r];
+            snsh[r] = a.sn[r];
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            ctl->reorth = 0;
+            ctl->lag_pending = ro ? 1 : 0;
+            if (ro)
+                ctl->reorth_count += 1;
+            finish_column_at(ctl, acc, cssh, snsh, a.cs, a.sn, a.g, a.s, beta,
+                             nf || !isfinite(nrm) || !isfinite(beta));
+        }
+        __syncthreads();
+        for (int j = threadIdx.x; j <= k + 1; j += blockDim.x)
+            colh[j] = acc[j];
         return;
     }
     if (threadIdx.x != 0)

@@ -127,16 +127,24 @@ DeviceDia<T> build_dia(DeviceArena &arena, const DeviceCsr<T> &m, int sms, cudaS
 }
 
 // y[row] = scale * sum_d val[d][row] x(row + off[d]) over the row's present diagonals, in
-// ascending offset order; one thread per row.
-template <class T, class XF>
+// ascending offset order; one thread per row. MAXD >= ndiag bounds a fully unrolled loop, so a
+// row's value and x loads are all issued before its sum (every load independent of the others).
+template <int MAXD, class T, class XF>
 __device__ __forceinline__ void dia_rows(const DeviceDia<T> &m, XF xget, T scale, T *__restrict__ y) {
     for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < m.n; row += gridDim.x * blockDim.x) {
         const unsigned mk = __ldg(m.mask + row);
+        T v[MAXD], x[MAXD];
+#pragma unroll
+        for (int d = 0; d < MAXD; ++d) {
+            const bool on = d < m.ndiag && ((mk >> d) & 1u);
+            v[d] = on ? __ldg(m.val + static_cast<long long>(d) * m.n + row) : T(0);
+            x[d] = on ? xget(row + m.off[d]) : T(0);
+        }
         T acc = 0;
-#pragma unroll 8
-        for (int d = 0; d < m.ndiag; ++d)
-            if ((mk >> d) & 1u)
-                acc += __ldg(m.val + static_cast<long long>(d) * m.n + row) * xget(row + m.off[d]);
+#pragma unroll
+        for (int d = 0; d < MAXD; ++d)
+            if (d < m.ndiag && ((mk >> d) & 1u))
+                acc += v[d] * x[d];
         y[row] = acc * scale;
     }
 }

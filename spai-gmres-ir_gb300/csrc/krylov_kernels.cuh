@@ -28,6 +28,7 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
 namespace spai {
@@ -768,15 +769,15 @@ DeviceSell<T> tuned_sell(DeviceArena &arena, const DeviceCsr<T> &m, int sms, cud
     return t_srt < t_nat ? srt : nat;
 }
 
-// Diagonal-layout SpMVs (stencil-like profiles, dia.cuh).
-template <class T>
+// Diagonal-layout SpMVs (stencil-like profiles, dia.cuh); MAXD: diagonals rounded up to 8.
+template <class T, int MAXD>
 __global__ void __launch_bounds__(kBlock) dia_spmv_kernel(DeviceDia<T> m, VecRef<T> x, VecRef<T> y, const int *gate) {
     if (gate && !*gate)
         return;
     const T *xv = x.get();
-    dia_rows(m, [&](int c) { return __ldg(xv + c); }, T(1), y.get());
+    dia_rows<MAXD>(m, [&](int c) { return __ldg(xv + c); }, T(1), y.get());
 }
-template <class T>
+template <class T, int MAXD>
 __global__ void __launch_bounds__(kBlock) dia_spmv_basis_kernel(DeviceDia<T> m, Basis<T> V, T *y, const Ctl *ctl) {
     constexpr int R = TileGeom<T>::R;
     if (!ctl->active)
@@ -784,7 +785,17 @@ __global__ void __launch_bounds__(kBlock) dia_spmv_basis_kernel(DeviceDia<T> m, 
     const int k = ctl->k;
     const T *base = V.base + static_cast<long long>(k) * R;
     const long long tstride = static_cast<long long>(V.cap1) * R;
-    dia_rows(m, [&](int c) { return base[(c / R) * tstride + (c % R)]; }, V.scale[k], y);
+    dia_rows<MAXD>(m, [&](int c) { return base[(c / R) * tstride + (c % R)]; }, V.scale[k], y);
+}
+template <class T, class F> void dia_dispatch(int ndiag, F &&launch) {
+    if (ndiag <= 8)
+        launch(std::integral_constant<int, 8>{});
+    else if (ndiag <= 16)
+        launch(std::integral_constant<int, 16>{});
+    else if (ndiag <= 24)
+        launch(std::integral_constant<int, 24>{});
+    else
+        launch(std::integral_constant<int, 32>{});
 }
 
 // A Krylov SpMV operand in the layout the tuner chose: sliced ELLPACK (natural or length-sorted
@@ -803,7 +814,9 @@ template <class T> struct KrylovOp {
 template <class T>
 void launch_op(const KrylovOp<T> &op, VecRef<T> x, VecRef<T> y, const int *gate, int sms, cudaStream_t st) {
     if (op.layout == 2) {
-        dia_spmv_kernel<T><<<grid_for(op.dia.n, kBlock, sms * 8), kBlock, 0, st>>>(op.dia, x, y, gate);
+        dia_dispatch<T>(op.dia.ndiag, [&](auto md) {
+            dia_spmv_kernel<T, decltype(md)::value><<<grid_for(op.dia.n, kBlock, sms * 8), kBlock, 0, st>>>(op.dia, x, y, gate);
+        });
         SPAI_LAUNCH("dia_spmv_kernel");
         return;
     }
@@ -811,7 +824,9 @@ void launch_op(const KrylovOp<T> &op, VecRef<T> x, VecRef<T> y, const int *gate,
 }
 template <class T> void launch_op_basis(const KrylovOp<T> &op, Basis<T> V, T *y, const Ctl *ctl, int sms, cudaStream_t st) {
     if (op.layout == 2) {
-        dia_spmv_basis_kernel<T><<<grid_for(op.dia.n, kBlock, sms * 8), kBlock, 0, st>>>(op.dia, V, y, ctl);
+        dia_dispatch<T>(op.dia.ndiag, [&](auto md) {
+            dia_spmv_basis_kernel<T, decltype(md)::value><<<grid_for(op.dia.n, kBlock, sms * 8), kBlock, 0, st>>>(op.dia, V, y, ctl);
+        });
         SPAI_LAUNCH("dia_spmv_basis_kernel");
         return;
     }
@@ -1205,7 +1220,9 @@ template <class T, class TO> struct IrEngine {
         SPAI_CUDA(cudaFuncSetAttribute(cgs_pass_kernel<T, 5>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
         // The lagged passes need every step to stream whole tiles (k + 2 <= stage_segs for
         // k < cap); SPAI_CGS_LAG=0 keeps the three-pass form (comparisons).
-        lag = cap + 1 <= stage_segs && !cgs_acc_global<T>(cap);
+        // (and the packed triangular factors of the finishing blocks fit in the staging region).
+        lag = cap + 1 <= stage_segs && !cgs_acc_global<T>(cap) &&
+              static_cast<size_t>(cap) * (cap + 3) / 2 * sizeof(T) <= static_cast<size_t>(kCgsStages) * stage_segs * 512;
         if (const char *e = std::getenv("SPAI_CGS_LAG"))
             lag = lag && std::atoi(e) != 0;
         w = arena.alloc<T>(ld);
