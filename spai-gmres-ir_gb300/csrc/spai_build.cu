@@ -574,13 +574,15 @@ __device__ int fit_column(const Grp &g, const ColumnArgs<T> &A, int k, char *ws,
             status = kRankDeficient;
             break;
         }
-        T *s = bump.take<T>(m);
-        const size_t keep_mark = bump.mark();
+        // Workspace of the fit: [I][R][rhs][v][coef]. The fitted residual s, which the candidate
+        // phase needs, is moved next to I once R is consumed, so it does not add to the peak of the
+        // least-squares phase (a column's last fit then fits a smaller workspace).
+        const size_t ls_mark = bump.mark();
         T *R = bump.take<T>(static_cast<long long>(m) * q);
         T *rhs = bump.take<T>(m);
         T *v = bump.take<T>(m);
         T *coef = bump.take<T>(q);
-        if (!s || !R || !rhs || !v || !coef)
+        if (!R || !rhs || !v || !coef)
             return kOverflow;
         gather_reduced(g, A, J, q, I, m, R);
         for (int i = lane; i < m; i += GS)
@@ -594,7 +596,8 @@ __device__ int fit_column(const Grp &g, const ColumnArgs<T> &A, int k, char *ws,
             status = ls;
             break;
         }
-        // Fitted residual with the original reduced matrix.
+        // Fitted residual with the original reduced matrix (into v, free after the fit), then moved
+        // to s right after I (over R's first rows: R is no longer needed; v lies beyond them).
         gather_reduced(g, A, J, q, I, m, R);
         int bad = 0;
         for (int i = lane; i < m; i += GS) {
@@ -602,13 +605,19 @@ __device__ int fit_column(const Grp &g, const ColumnArgs<T> &A, int k, char *ws,
             for (int jj = 0; jj < q; ++jj)
                 acc += R[static_cast<long long>(i) * q + jj] * coef[jj];
             acc -= (I[i] == k ? T(1) : T(0));
-            s[i] = acc;
+            v[i] = acc;
             bad |= !isfinite(acc);
         }
         if (g.any(bad)) {
             status = kNumericalFailure;
             break;
         }
+        g.sync();
+        bump.reset(ls_mark);
+        T *s = bump.take<T>(m);
+        const size_t keep_mark = bump.mark();
+        for (int i = lane; i < m; i += GS)
+            s[i] = v[i];
         g.sync();
         T res = 0;
         if (FAST) {
@@ -1086,10 +1095,15 @@ struct TierPlan {
 // that do not fit move up the chain and are fitted again from the start (fits are deterministic,
 // so the result does not depend on the tier that completes a column).
 inline std::vector<TierPlan> plan_tiers(size_t first_ws, int first_G, int max_threads, size_t smem_budget,
-                                        int first_qcap) {
+                                        int first_qcap, size_t elem = 4) {
     std::vector<TierPlan> tiers;
-    auto qcap_for = [](size_t ws) {
-        return ws <= 4096 ? 32 : (ws <= 16384 ? 64 : (ws <= 65536 ? 256 : 1024));
+    // Pattern capacity by workspace: up to 1,536 values (6 KiB of binary32, 12 KiB of binary64)
+    // the fits are small (a 3-D stencil column ends near 17-25 pattern entries), so 32 entries
+    // keep the per-group header (J, last J, last coefficients) small; a column that outgrows it
+    // moves up a tier.
+    auto qcap_for = [elem](size_t ws) {
+        const size_t vals = ws / elem;
+        return vals <= 1536 ? 32 : (vals <= 4096 ? 64 : (vals <= 16384 ? 256 : 1024));
     };
     const size_t last_shared = smem_budget / 4;
     size_t ws = first_ws;
@@ -1152,9 +1166,9 @@ TuneChoice tune_first_tier(const DeviceCsr<T> &a, const SpaiParams &prm, bool he
     if (heavy)
         cands = {{G_def, ws_def}, {32, 28672}, {16, 14336}, {32, 57344}, {8, 14336}};
     else if (sizeof(T) == 4)
-        cands = {{G_def, ws_def}, {8, 4096}, {8, 3072}, {4, 3072}, {8, 6144}, {16, 10240}};
+        cands = {{G_def, ws_def}, {8, 4800}, {8, 4352}, {8, 4096}, {8, 3072}, {4, 3072}, {8, 6144}, {16, 10240}};
     else
-        cands = {{G_def, ws_def}, {8, 10240}, {8, 8192}, {4, 8192}, {16, 12288}};
+        cands = {{G_def, ws_def}, {8, 10240}, {8, 9216}, {8, 8704}, {8, 8192}, {4, 8192}, {16, 12288}};
     args.phase = nullptr;
     DeviceArena mem; // sample list and global workspaces of the sample runs (freed on return)
     int *list = mem.alloc<int>(S);
@@ -1172,7 +1186,7 @@ TuneChoice tune_first_tier(const DeviceCsr<T> &a, const SpaiParams &prm, bool he
         const size_t ws = cands[c].second;
         if (ws > smem_budget || G * 4 > max_threads)
             continue;
-        const std::vector<TierPlan> tiers = plan_tiers(ws, G, max_threads, smem_budget, 0);
+        const std::vector<TierPlan> tiers = plan_tiers(ws, G, max_threads, smem_budget, 0, sizeof(T));
         SPAI_CUDA(cudaMemsetAsync(queue, 0, sizeof(int) * 64, st));
         SPAI_CUDA(cudaMemcpyAsync(&queue[62], &S, sizeof(int), cudaMemcpyHostToDevice, st));
         SPAI_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
@@ -1273,7 +1287,16 @@ void SpaiBuilder<T>::construct(const DeviceCsr<T> &a, const SpaiParams &prm, cud
     const size_t ws_def = heavy ? 28672 : (sizeof(T) == 8 ? 12288 : 5120);
     int G0 = prm.group_lanes > 0 ? prm.group_lanes : G_def;
     size_t ws0 = prm.ws_bytes_per_warp > 0 ? static_cast<size_t>(prm.ws_bytes_per_warp) : ws_def;
-    const size_t smem_budget = 225 * 1024;
+    // Shared memory of one block: the device's per-block maximum (the kernel has no static shared
+    // memory), less a small margin.
+    size_t smem_budget = 225 * 1024;
+    {
+        int dev0 = 0, optin = 0;
+        SPAI_CUDA(cudaGetDevice(&dev0));
+        SPAI_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev0));
+        if (optin > 64 * 1024)
+            smem_budget = static_cast<size_t>(optin) - 256;
+    }
     // Threads per block within the register budget of one block (124 registers/thread for
     // binary64, 77 for binary32 -> at most 512 / 768 threads).
     const int max_threads = sizeof(T) == 8 ? 512 : 768;
@@ -1360,7 +1383,7 @@ void SpaiBuilder<T>::construct(const DeviceCsr<T> &a, const SpaiParams &prm, cud
                 out.tune_default_ms = c.default_ms;
             }
         }
-        const std::vector<TierPlan> tiers = plan_tiers(ws0, G0, max_threads, smem_budget, prm.first_qcap);
+        const std::vector<TierPlan> tiers = plan_tiers(ws0, G0, max_threads, smem_budget, prm.first_qcap, sizeof(T));
         out.group_lanes = tiers[0].G;
         out.ws_bytes = static_cast<int>(tiers[0].ws);
         run_chain(tiers, args, nullptr, n, arena, trace, out.overflow_columns, out.overflow_columns_global);
