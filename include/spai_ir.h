@@ -117,7 +117,8 @@ typedef struct {
                                    not verified (candidates are formed only when the acceptance
                                    rule can accept them) */
     int32_t accepted;
-    int32_t pad;
+    int32_t triggered;          /* the acceptance rule's check was due at this step (estimate <= tau,
+                                   breakdown or the cap; GmresIteration::verification_triggered) */
 } spai_iteration_record;
 
 /* Canonical CSR on the host (row_offsets[n+1], sorted col_indices[nnz], no stored zeros), the
@@ -212,6 +213,51 @@ int spai_spmv(spai_handle *h, int32_t which, const double *x, double *y);
  * out_status = GMRES_*, out_iterations, out_relative = recomputed preconditioned residual. */
 int spai_gmres(spai_handle *h, const double *rhs, double *x, double tau, int64_t cap,
                int32_t *out_status, int64_t *out_iterations, double *out_relative);
+
+/* Caller-supplied preconditioner (canonical CSR, n x n) in place of a SPAI build: the handle then
+ * solves with P as refine_with_preconditioner and left_preconditioned_gmres do with a fixed P
+ * (include/bspai/ir.hpp:63-65, include/bspai/gmres.hpp:55-57). P is kept in the handle's working
+ * precision; the SPAI column queries (spai_get_columns, spai_get_column) then return
+ * SPAI_ERR_NOT_BUILT. */
+int spai_set_preconditioner(spai_handle *h, const spai_csr *p);
+
+/* Record mode of a binary64 handle (enable != 0; SPAI_ERR_ARGUMENT for other precisions): the
+ * next spai_build logs every fit of every column (spai_fit_log), and every later spai_solve and
+ * spai_gmres runs its refinement loop from the host one Arnoldi step at a time in the three-pass
+ * Gram-Schmidt form, forms and checks every step's candidate (only a triggered check may accept
+ * it, gmres.cpp:235-240, so results equal the unrecorded solve's up to the three-pass
+ * orthogonalisation) and keeps what the reference's GmresResult and IrResult histories hold
+ * (include/bspai/gmres.hpp:28-50, ir.hpp:36-56): every step's candidate, the basis, the
+ * unrotated Hessenberg, every iterate and residual. Diagnostics for small systems; the records
+ * live in host memory of the handle until the next recorded solve. No reference counterpart
+ * beyond those result structures (the reference's release snapshot prints them,
+ * tests/release_cpu_snapshot.cpp:281-398). */
+int spai_record(spai_handle *h, int32_t enable);
+/* Fit log of the last build in record mode: an int stream and a binary64 stream of records, each
+ * with an 8-int header (kind, column, workspace tier, fit ordinal, a, b, c, offset of its values):
+ * kind 1 (fit): a = |J|, b = |I|; ints J then I; values residual, pivot ratio, coefficients;
+ * kind 2 (candidate scores): a = candidates, b = selected, c = room; ints candidates then the
+ * selection (in selection order, b used of c); values mean score, then one score per candidate.
+ * A column refitted from scratch in a larger workspace tier logs again under the higher tier;
+ * only its highest tier's records are its history. n_ints / n_vals give the stream lengths;
+ * SPAI_ERR_WORKSPACE when the log overflowed. */
+int spai_fit_log(spai_handle *h, int32_t *ints, int64_t max_ints, int64_t *n_ints, double *vals,
+                 int64_t max_vals, int64_t *n_vals);
+/* Counts of the last recorded solve: iterates kept (x0 = P b and one per applied correction) and
+ * inner GMRES solves (one for spai_gmres). */
+int spai_record_counts(spai_handle *h, int64_t *n_states, int64_t *n_inner);
+/* Iterate s of the last recorded solve and its residual b - A x (n each; either may be NULL). */
+int spai_record_state(spai_handle *h, int64_t s, double *x, double *residual);
+/* Inner solve i of the last recorded solve; any output may be NULL.
+ * summary[12]: gmres status, converged, steps m, correction applied, ||rhs||, initial relative
+ *   residual (1: zero initial guess), final original residual, final preconditioned relative
+ *   residual, basis vectors kept nb, Hessenberg rows (cap + 1), columns (cap), iterations;
+ * rhs[n], solution[n] (the last candidate, zero without steps), basis[nb * n] (normalised
+ * v_j = s_j W_j, row j = vector j), hessenberg[(cap + 1) * cap] (unrotated, row-major),
+ * steps[m * 8] (iteration, estimate, recomputed relative, original residual, subdiagonal,
+ * breakdown, verification triggered, accepted), candidates[m * n] (each step's candidate). */
+int spai_record_inner(spai_handle *h, int64_t i, double *summary, double *rhs, double *solution, double *basis,
+                      double *hessenberg, double *steps, double *candidates);
 
 /* Score guard KAT on the device (cuda_evaluate_spai_score). out = {status, score, clamped}. */
 int spai_score(int32_t precision, double rsq, double dot, double den, double *out);

@@ -128,6 +128,10 @@ struct spai_handle_s {
     int hist_n_outer = 0, hist_n_inner = 0, hist_n_iter = 0;
     int hist_cap_outer = 0, hist_cap_inner = 0, hist_cap_iter = 0;
     KernelProfile prof;
+    // Record mode (spai_record): fit log of the next builds, step records of the next solves.
+    bool recording = false;
+    KrylovRecord krec;
+    bool p_supplied = false; // P came from spai_set_preconditioner (no SPAI columns)
     double spai_ms = 0;
     long long spai_launches = 0;
 
@@ -343,7 +347,14 @@ int solve_device_impl(spai_handle *h, const double *d_b, double *d_x, const spai
     }
     const int cap = o.innercap == 0 ? h->n : static_cast<int>(o.innercap);
     ensure_engine(h, cap);
-    run_solve(h, h->e64, h->emix, h->e32, d_b, d_x, settings_for(h, o, cap), rep);
+    SolveSettings s = settings_for(h, o, cap);
+    if (h->recording) { // record mode: host-driven loop, every step read back (binary64 handles)
+        h->krec.clear();
+        s.record = &h->krec;
+        s.history = true;
+        s.use_graph = false;
+    }
+    run_solve(h, h->e64, h->emix, h->e32, d_b, d_x, s, rep);
     rep->nnz_p = h->precision == SPAI_PREC_F64 ? h->s64.p.nnz : h->s32.p.nnz;
     return SPAI_OK;
 }
@@ -425,6 +436,38 @@ int adjoint_device_impl(spai_handle *h, int nrhs, const double *d_x, const doubl
 
 } // namespace spai_api
 
+namespace spai_api {
+// Canonical host CSR -> device CSR in `dst` (64-bit indices narrowed on the device through the
+// handle's scratch arena); stream-ordered.
+DeviceCsr<double> upload_csr(spai_handle *h, DeviceArena &dst, const spai_csr *a) {
+    const int n = static_cast<int>(a->n), nnz = static_cast<int>(a->nnz);
+    DeviceCsr<double> m;
+    m.n = n;
+    m.nnz = nnz;
+    int max_row = 0;
+    for (int64_t r = 0; r < a->n; ++r)
+        max_row = std::max<int>(max_row, static_cast<int>(a->row_offsets[r + 1] - a->row_offsets[r]));
+    m.max_row = max_row;
+    m.rp = dst.alloc<int>(n + 1);
+    m.ci = dst.alloc<int>(nnz > 0 ? nnz : 1);
+    m.val = dst.alloc<double>(nnz > 0 ? nnz : 1);
+    h->scratch.reset();
+    long long *tmp = h->scratch.alloc<long long>(std::max(n + 1, nnz));
+    cudaStream_t st = h->stream;
+    SPAI_CUDA(cudaMemcpyAsync(tmp, a->row_offsets, sizeof(long long) * (n + 1), cudaMemcpyHostToDevice, st));
+    narrow_kernel<<<grid_for(n + 1, 256, h->sms * 8), 256, 0, st>>>(n + 1, tmp, m.rp);
+    SPAI_LAUNCH("narrow_kernel");
+    if (nnz > 0) {
+        // The index copy reuses tmp after the row offsets are narrowed (stream order).
+        SPAI_CUDA(cudaMemcpyAsync(tmp, a->col_indices, sizeof(long long) * nnz, cudaMemcpyHostToDevice, st));
+        narrow_kernel<<<grid_for(nnz, 256, h->sms * 8), 256, 0, st>>>(nnz, tmp, m.ci);
+        SPAI_LAUNCH("narrow_kernel");
+        SPAI_CUDA(cudaMemcpyAsync(m.val, a->values, sizeof(double) * nnz, cudaMemcpyHostToDevice, st));
+    }
+    return m;
+}
+} // namespace spai_api
+
 extern "C" {
 
 int spai_default_options(spai_options *opt, int32_t precision) {
@@ -458,6 +501,7 @@ const char *spai_last_error(void) {
     return g_last_error.c_str();
 }
 
+
 int spai_create(const spai_csr *a, int32_t precision, int device, void *stream, spai_handle **out) {
     API_BEGIN
     if (!out || precision < 0 || precision > 2)
@@ -481,30 +525,12 @@ int spai_create(const spai_csr *a, int32_t precision, int device, void *stream, 
     }
     SPAI_CUDA(cudaMallocHost(&h->pinned, 64));
     const int n = h->n, nnz = h->nnz;
-    int max_row = 0;
-    for (int64_t r = 0; r < a->n; ++r)
-        max_row = std::max<int>(max_row, static_cast<int>(a->row_offsets[r + 1] - a->row_offsets[r]));
-    h->a64.n = n;
-    h->a64.nnz = nnz;
-    h->a64.max_row = max_row;
-    h->a64.rp = h->mat.alloc<int>(n + 1);
-    h->a64.ci = h->mat.alloc<int>(nnz);
-    h->a64.val = h->mat.alloc<double>(nnz);
-    long long *tmp = h->scratch.alloc<long long>(std::max(n + 1, nnz));
     cudaStream_t st = h->stream;
-    SPAI_CUDA(cudaMemcpyAsync(tmp, a->row_offsets, sizeof(long long) * (n + 1), cudaMemcpyHostToDevice, st));
-    narrow_kernel<<<grid_for(n + 1, 256, h->sms * 8), 256, 0, st>>>(n + 1, tmp, h->a64.rp);
-    SPAI_LAUNCH("narrow_kernel");
-    if (nnz > 0) {
-        SPAI_CUDA(cudaMemcpyAsync(tmp, a->col_indices, sizeof(long long) * nnz, cudaMemcpyHostToDevice, st));
-        narrow_kernel<<<grid_for(nnz, 256, h->sms * 8), 256, 0, st>>>(nnz, tmp, h->a64.ci);
-        SPAI_LAUNCH("narrow_kernel");
-        SPAI_CUDA(cudaMemcpyAsync(h->a64.val, a->values, sizeof(double) * nnz, cudaMemcpyHostToDevice, st));
-    }
+    h->a64 = upload_csr(h.get(), h->mat, a);
     if (precision != SPAI_PREC_F64) {
         h->a32.n = n;
         h->a32.nnz = nnz;
-        h->a32.max_row = max_row;
+        h->a32.max_row = h->a64.max_row;
         h->a32.rp = h->a64.rp;
         h->a32.ci = h->a64.ci;
         h->a32.val = h->mat.alloc<float>(nnz);
@@ -537,6 +563,7 @@ int spai_build(spai_handle *h, const spai_options *opt, spai_report *rep) {
     clear_report(rep);
     SPAI_CUDA(cudaSetDevice(h->device));
     h->built = false;
+    h->p_supplied = false;
     h->engine_cap = -1;
     h->adj_ready = false;
     h->adj_cap = -1;
@@ -551,6 +578,7 @@ int spai_build(spai_handle *h, const spai_options *opt, spai_report *rep) {
         prm.first_qcap = std::atoi(e);
     if (const char *e = std::getenv("SPAI_TUNE"))
         prm.tune = std::atoi(e) != 0;
+    prm.record = h->recording;
     prm.epsilon = opt->epsilon;
     // Every form follows the reference's sequential arithmetic bit for bit by default; the
     // group-parallel variant (parallel norms and mean, hashed candidate sets) is opt-in.
@@ -745,6 +773,8 @@ int spai_get_columns(spai_handle *h, int32_t *status, int32_t *fits, int32_t *gr
         return fail(SPAI_ERR_NOT_BUILT, "no preconditioner built");
     const int n = h->n;
     const bool f64 = h->precision == SPAI_PREC_F64;
+    if (h->p_supplied)
+        return fail(SPAI_ERR_NOT_BUILT, "no SPAI columns (the preconditioner was supplied by the caller)");
     auto get_i = [&](int32_t *dst, const int *src) {
         if (dst && src)
             SPAI_CUDA(cudaMemcpy(dst, src, sizeof(int) * n, cudaMemcpyDeviceToHost));
@@ -790,6 +820,8 @@ int spai_get_column(spai_handle *h, int64_t k, int64_t *q, int64_t *pattern, dou
     long long off = -1;
     const int *cq = f64 ? h->s64.col_q : h->s32.col_q;
     const long long *co = f64 ? h->s64.packed_off : h->s32.packed_off;
+    if (h->p_supplied)
+        return fail(SPAI_ERR_NOT_BUILT, "no SPAI columns (the preconditioner was supplied by the caller)");
     if (!cq) {
         *q = 0;
         return SPAI_OK;
@@ -886,6 +918,10 @@ int spai_gmres(spai_handle *h, const double *rhs, double *x, double tau, int64_t
     s.cap = c;
     s.tau = tau;
     s.accept_every = h->precision == SPAI_PREC_F32;
+    if (h->recording) {
+        h->krec.clear();
+        s.record = &h->krec;
+    }
     h->scratch.reset();
     double *dr = h->scratch.alloc<double>(n);
     double *dx = h->scratch.alloc<double>(n);
@@ -948,6 +984,150 @@ int spai_history(spai_handle *h, spai_outer_record *outer, int64_t max_outer, in
         *n_iterations = h->hist_n_iter;
     return SPAI_OK;
     API_END
+}
+
+int spai_set_preconditioner(spai_handle *h, const spai_csr *p) {
+    API_BEGIN
+    if (!h || !p)
+        return fail(SPAI_ERR_ARGUMENT, "spai_set_preconditioner: null argument");
+    const std::string why = canonical_error(p);
+    if (!why.empty())
+        return fail(SPAI_ERR_ARGUMENT, "spai_set_preconditioner: " + why);
+    if (p->n != h->n)
+        return fail(SPAI_ERR_ARGUMENT, "spai_set_preconditioner: P and A differ in dimension");
+    SPAI_CUDA(cudaSetDevice(h->device));
+    SPAI_CUDA(cudaStreamSynchronize(h->stream));
+    h->built = false;
+    h->engine_cap = -1;
+    h->adj_ready = false;
+    h->adj_cap = -1;
+    h->build.reset();
+    const DeviceCsr<double> p64 = upload_csr(h, h->build, p);
+    if (h->precision == SPAI_PREC_F64) {
+        h->s64 = SpaiOutput<double>{};
+        h->s64.n = h->n;
+        h->s64.status = SPAI_SUCCESS;
+        h->s64.p = p64;
+    } else {
+        h->s32 = SpaiOutput<float>{};
+        h->s32.n = h->n;
+        h->s32.status = SPAI_SUCCESS;
+        h->s32.p.n = p64.n;
+        h->s32.p.nnz = p64.nnz;
+        h->s32.p.max_row = p64.max_row;
+        h->s32.p.rp = p64.rp;
+        h->s32.p.ci = p64.ci;
+        h->s32.p.val = h->build.alloc<float>(p64.nnz > 0 ? p64.nnz : 1);
+        if (p64.nnz > 0) {
+            convert_kernel<float, double><<<grid_for(p64.nnz, 256, h->sms * 8), 256, 0, h->stream>>>(p64.nnz, p64.val,
+                                                                                               h->s32.p.val);
+            SPAI_LAUNCH("convert_kernel");
+        }
+    }
+    SPAI_CUDA(cudaStreamSynchronize(h->stream));
+    h->spai_status = SPAI_SUCCESS;
+    h->spai_ms = 0;
+    h->built = true;
+    h->p_supplied = true;
+    return SPAI_OK;
+    API_END
+}
+
+int spai_record(spai_handle *h, int32_t enable) {
+    API_BEGIN
+    if (!h)
+        return fail(SPAI_ERR_ARGUMENT, "spai_record: null handle");
+    if (enable && h->precision != SPAI_PREC_F64)
+        return fail(SPAI_ERR_ARGUMENT, "spai_record: record mode is binary64 only");
+    h->recording = enable != 0;
+    h->krec.clear();
+    return SPAI_OK;
+    API_END
+}
+
+int spai_fit_log(spai_handle *h, int32_t *ints, int64_t max_ints, int64_t *n_ints, double *vals,
+                 int64_t max_vals, int64_t *n_vals) {
+    API_BEGIN
+    if (!h)
+        return fail(SPAI_ERR_ARGUMENT, "spai_fit_log: null handle");
+    if (!h->built || !h->s64.log_top)
+        return fail(SPAI_ERR_NOT_BUILT, "no fit log: the last build did not run in record mode");
+    unsigned long long top[2] = {0, 0};
+    SPAI_CUDA(cudaMemcpy(top, h->s64.log_top, sizeof(top), cudaMemcpyDeviceToHost));
+    if (static_cast<long long>(top[0]) > h->s64.log_int_cap || static_cast<long long>(top[1]) > h->s64.log_val_cap)
+        return fail(SPAI_ERR_WORKSPACE, "the fit log overflowed its capacity");
+    if (n_ints)
+        *n_ints = static_cast<int64_t>(top[0]);
+    if (n_vals)
+        *n_vals = static_cast<int64_t>(top[1]);
+    if (ints && max_ints > 0)
+        SPAI_CUDA(cudaMemcpy(ints, h->s64.log_ints, sizeof(int32_t) * std::min<int64_t>(max_ints, top[0]),
+                             cudaMemcpyDeviceToHost));
+    if (vals && max_vals > 0)
+        SPAI_CUDA(cudaMemcpy(vals, h->s64.log_vals, sizeof(double) * std::min<int64_t>(max_vals, top[1]),
+                             cudaMemcpyDeviceToHost));
+    return SPAI_OK;
+    API_END
+}
+
+int spai_record_counts(spai_handle *h, int64_t *n_states, int64_t *n_inner) {
+    if (!h)
+        return fail(SPAI_ERR_ARGUMENT, "spai_record_counts: null handle");
+    if (n_states)
+        *n_states = static_cast<int64_t>(h->krec.states.size());
+    if (n_inner)
+        *n_inner = static_cast<int64_t>(h->krec.inner.size());
+    return SPAI_OK;
+}
+
+int spai_record_state(spai_handle *h, int64_t s, double *x, double *residual) {
+    if (!h || s < 0 || s >= static_cast<int64_t>(h->krec.states.size()))
+        return fail(SPAI_ERR_ARGUMENT, "spai_record_state: no such state");
+    const KrylovState &st = h->krec.states[static_cast<size_t>(s)];
+    if (x)
+        std::copy(st.x.begin(), st.x.end(), x);
+    if (residual)
+        std::copy(st.residual.begin(), st.residual.end(), residual);
+    return SPAI_OK;
+}
+
+int spai_record_inner(spai_handle *h, int64_t i, double *summary, double *rhs, double *solution, double *basis,
+                      double *hessenberg, double *steps, double *candidates) {
+    if (!h || i < 0 || i >= static_cast<int64_t>(h->krec.inner.size()))
+        return fail(SPAI_ERR_ARGUMENT, "spai_record_inner: no such inner solve");
+    const KrylovInner &in = h->krec.inner[static_cast<size_t>(i)];
+    const int m = static_cast<int>(in.steps.size());
+    if (summary) {
+        const double sm[12] = {static_cast<double>(in.status), static_cast<double>(in.converged),
+                               static_cast<double>(m),         static_cast<double>(in.applied),
+                               in.initial_original,            1.0,
+                               in.final_original,              in.final_preconditioned,
+                               static_cast<double>(in.nbasis), static_cast<double>(in.hcap + 1),
+                               static_cast<double>(in.hcap),   static_cast<double>(in.iterations)};
+        std::copy(sm, sm + 12, summary);
+    }
+    if (rhs)
+        std::copy(in.rhs.begin(), in.rhs.end(), rhs);
+    if (solution)
+        std::copy(in.solution.begin(), in.solution.end(), solution);
+    if (basis)
+        std::copy(in.basis.begin(), in.basis.end(), basis);
+    if (hessenberg)
+        std::copy(in.hessenberg.begin(), in.hessenberg.end(), hessenberg);
+    for (int k = 0; k < m; ++k) {
+        const spai_iteration_record &r = in.records[static_cast<size_t>(k)];
+        const double sub = in.hessenberg[static_cast<size_t>(k + 1) * in.hcap + k];
+        if (steps) {
+            const double row[8] = {static_cast<double>(k + 1), r.estimated_relative, r.recomputed_relative,
+                                   in.steps[static_cast<size_t>(k)].original, sub, sub == 0 ? 1.0 : 0.0,
+                                   static_cast<double>(r.triggered), static_cast<double>(r.accepted)};
+            std::copy(row, row + 8, steps + static_cast<size_t>(k) * 8);
+        }
+        if (candidates)
+            std::copy(in.steps[static_cast<size_t>(k)].candidate.begin(), in.steps[static_cast<size_t>(k)].candidate.end(),
+                      candidates + static_cast<size_t>(k) * h->n);
+    }
+    return SPAI_OK;
 }
 
 int spai_profile(spai_handle *h, int32_t enable) {

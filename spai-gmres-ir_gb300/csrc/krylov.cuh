@@ -3,6 +3,9 @@
 #include "spai_internal.hpp"
 #include "spai_ir.h"
 
+#include <cmath>
+#include <vector>
+
 namespace spai {
 
 // Control block in device memory. Every kernel of the Arnoldi step and the refinement loop
@@ -55,9 +58,45 @@ struct Ctl {
     int h_cap_outer, h_cap_inner, h_cap_iter;
     int h_n_outer, h_n_inner, h_n_iter;
     int h_iter_base;
+    // Record mode (SPAI_FLAG_RECORD): every step's candidate is formed and verified for the
+    // record, only a triggered check may accept it; h_raw (element type of the engine, leading
+    // dimension h_raw_ld) receives each Hessenberg column before its rotations.
+    int record_every;
+    int h_raw_ld;
+    void *h_raw;
 };
 
 struct GmresBuffers; // defined in krylov.cu
+
+// Host record of a solve run in record mode: what the reference's GmresResult and IrResult keep
+// (include/bspai/gmres.hpp:28-50, include/bspai/ir.hpp:36-56), as the device computed it, read
+// back after every Arnoldi step. Diagnostics for small systems.
+struct KrylovStep {
+    double original = NAN;          // ||rhs - A x_j|| of the step's candidate
+    std::vector<double> candidate;  // x_j = V_j y_j (zero initial guess)
+};
+struct KrylovInner {
+    int status = -1, converged = 0, iterations = 0, applied = 0;
+    double initial_original = NAN, final_original = NAN, final_preconditioned = NAN;
+    std::vector<double> rhs, solution;
+    std::vector<double> basis;       // nbasis normalised vectors of n entries
+    int nbasis = 0;
+    std::vector<double> hessenberg;  // unrotated, (cap + 1) x cap row-major
+    int hcap = 0;
+    std::vector<KrylovStep> steps;
+    std::vector<spai_iteration_record> records; // estimate, recomputed, trigger, acceptance
+};
+struct KrylovState {
+    std::vector<double> x, residual; // iterate and b - A x (binary64)
+};
+struct KrylovRecord {
+    std::vector<KrylovState> states;
+    std::vector<KrylovInner> inner;
+    void clear() {
+        states.clear();
+        inner.clear();
+    }
+};
 
 // Settings of one solve.
 struct SolveSettings {
@@ -70,6 +109,7 @@ struct SolveSettings {
     bool use_graph = true;
     bool history = false;      // record the refinement history (SPAI_FLAG_HISTORY)
     bool restart_at_cap = false; // SPAI_FLAG_RESTART_AT_CAP
+    struct KrylovRecord *record = nullptr; // SPAI_FLAG_RECORD: host record of every step
 };
 
 } // namespace spai

@@ -285,11 +285,13 @@ __global__ void decide_kernel(Ctl *ctl, const T *orig, const T *relnum) {
         const double rel = static_cast<double>(*relnum) / ctl->den;
         ctl->rel = rel;
         ctl->orig = static_cast<double>(*orig);
+        // Record mode checks every candidate; only a triggered check decides (gmres.cpp:235-240).
+        const bool decides = ctl->triggered != 0 || !ctl->record_every;
         if (ctl->h_iter) {
             const int idx = ctl->h_iter_base + ctl->k;
             if (idx < ctl->h_cap_iter) {
                 ctl->h_iter[idx].recomputed_relative = rel;
-                ctl->h_iter[idx].accepted = isfinite(rel) && rel <= ctl->tol_inner &&
+                ctl->h_iter[idx].accepted = decides && isfinite(rel) && rel <= ctl->tol_inner &&
                                             !(ctl->triggered == 2 && ctl->accept_every);
             }
         }
@@ -299,19 +301,19 @@ __global__ void decide_kernel(Ctl *ctl, const T *orig, const T *relnum) {
             return;
         }
         const bool ok = rel <= ctl->tol_inner;
-        if (ctl->triggered == 2) { // zero Givens pivot
+        if (decides && ctl->triggered == 2) { // zero Givens pivot
             ctl->converged = ok && !accept_every;
             ctl->status = ctl->converged ? 0 : 5;
             ctl->active = 0;
             return;
         }
-        if (ok) {
+        if (decides && ok) {
             ctl->converged = 1;
             ctl->status = 0;
             ctl->active = 0;
             return;
         }
-        if (ctl->breakdown) {
+        if (decides && ctl->breakdown) {
             ctl->status = 5;
             ctl->active = 0;
             return;
@@ -968,6 +970,8 @@ template <class T, class TO> struct IrEngine {
     // unrotated Hessenberg (see cgs_tiles.cuh).
     T *dl = nullptr, *fco = nullptr, *ecorr = nullptr, *Hu = nullptr, *Ui = nullptr, *yc = nullptr;
     bool lag = false; // two basis reads per Arnoldi step (every step of the solve streams)
+    T *Hraw = nullptr;          // record mode: Hessenberg columns before their rotations
+    KrylovRecord *rec = nullptr; // record mode: host record of the running solve
     TO *r = nullptr, *xn = nullptr;
     NormPart *npart = nullptr;
     DiagPart *dpart = nullptr;
@@ -1250,6 +1254,7 @@ template <class T, class TO> struct IrEngine {
         ecorr = arena.alloc<T>(cap + 2);
         yc = arena.alloc<T>(cap + 2);
         Hu = arena.alloc<T>(static_cast<size_t>(hld) * (cap + 1));
+        Hraw = arena.alloc<T>(static_cast<size_t>(hld) * (cap + 1));
         Ui = arena.alloc<T>(static_cast<size_t>(hld) * (cap + 2));
         part = arena.alloc<T>(static_cast<size_t>(std::max(nblk_dots, nblk_vec)) * (cap + 2));
         npart = arena.alloc<NormPart>(std::max(nblk_dots, nblk_vec));
@@ -1410,10 +1415,110 @@ template <class T, class TO> struct IrEngine {
         return *host_flag;
     }
 
+    // ---- Record mode: every step's candidate and the solve's basis and Hessenberg, read back ----
+    template <class U> std::vector<double> fetch(cudaStream_t st, const U *src, size_t count) {
+        std::vector<U> tmp(count);
+        if (count)
+            SPAI_CUDA(cudaMemcpyAsync(tmp.data(), src, count * sizeof(U), cudaMemcpyDeviceToHost, st));
+        SPAI_CUDA(cudaStreamSynchronize(st));
+        return std::vector<double>(tmp.begin(), tmp.end());
+    }
+    Ctl fetch_ctl(cudaStream_t st) {
+        Ctl c;
+        SPAI_CUDA(cudaMemcpyAsync(&c, ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
+        SPAI_CUDA(cudaStreamSynchronize(st));
+        return c;
+    }
+    void arm_record(Ctl &h, const SolveSettings &s) {
+        rec = s.record;
+        h.record_every = rec ? 1 : 0;
+        h.h_raw = rec ? static_cast<void *>(Hraw) : nullptr;
+        h.h_raw_ld = hld;
+    }
+    // After gmres_start: the correction right-hand side and its norm.
+    void record_inner_begin(cudaStream_t st) {
+        KrylovInner in;
+        in.rhs = fetch(st, rhs, n);
+        in.initial_original = fetch(st, scal + 2, 1)[0];
+        rec->inner.push_back(std::move(in));
+    }
+    // One step at a time, so that exactly the executed steps are recorded.
+    void gmres_loop_record(cudaStream_t st, int *pinned) {
+        pinned_host = pinned + 1;
+        host_k = 0;
+        for (int it = 0; it < cap; ++it) {
+            if (!read_flag(st, pinned, &ctl->active))
+                break;
+            arnoldi_step(st);
+            KrylovStep sr;
+            sr.candidate = fetch(st, cand, n);
+            sr.original = fetch(st, scal + 0, 1)[0];
+            rec->inner.back().steps.push_back(std::move(sr));
+        }
+    }
+    // After the inner loop (before the refinement advances the history base): status, norms,
+    // the step records, the unrotated Hessenberg and the normalised basis v_j = s_j W_j.
+    void record_inner_end(cudaStream_t st) {
+        KrylovInner &in = rec->inner.back();
+        const Ctl c = fetch_ctl(st);
+        in.status = c.status;
+        in.converged = c.converged;
+        in.iterations = c.iterations;
+        in.final_original = c.orig;
+        in.final_preconditioned = c.rel;
+        const int m = static_cast<int>(in.steps.size());
+        in.records.assign(m, spai_iteration_record{});
+        if (m > 0 && hist_iter && c.h_iter_base + m <= hist_cap_iter)
+            SPAI_CUDA(cudaMemcpyAsync(in.records.data(), hist_iter + c.h_iter_base, sizeof(spai_iteration_record) * m,
+                                      cudaMemcpyDeviceToHost, st));
+        const std::vector<double> raw = fetch(st, Hraw, static_cast<size_t>(hld) * (cap + 1));
+        in.hcap = cap;
+        in.hessenberg.assign(static_cast<size_t>(cap + 1) * cap, 0.0);
+        for (int k = 0; k < m; ++k)
+            for (int r = 0; r <= k + 1; ++r)
+                in.hessenberg[static_cast<size_t>(r) * cap + k] = raw[static_cast<size_t>(k) * hld + r];
+        // v_0, and v_{k+1} after every step whose subdiagonal is nonzero (gmres.cpp:184-190).
+        in.nbasis = m == 0 ? 0 : m + (raw[static_cast<size_t>(m - 1) * hld + m] != 0 ? 1 : 0);
+        in.nbasis = std::min(in.nbasis, cap + 1);
+        if (in.nbasis > 0) {
+            constexpr int R = TileGeom<T>::R;
+            const std::vector<double> tiles = fetch(st, V, static_cast<size_t>(ntiles) * (cap + 1) * R);
+            const std::vector<double> scl = fetch(st, sc, cap + 2);
+            in.basis.assign(static_cast<size_t>(in.nbasis) * n, 0.0);
+            for (int j = 0; j < in.nbasis; ++j)
+                for (int i = 0; i < n; ++i)
+                    in.basis[static_cast<size_t>(j) * n + i] =
+                        static_cast<double>(static_cast<T>(scl[j]) *
+                                            static_cast<T>(tiles[(static_cast<size_t>(i / R) * (cap + 1) + j) * R + i % R]));
+        }
+        in.solution = m > 0 ? in.steps.back().candidate : std::vector<double>(n, 0.0);
+    }
+    void record_state(cudaStream_t st, const TO *x) {
+        KrylovState sr;
+        sr.x = fetch(st, x, n);
+        sr.residual = fetch(st, r, n);
+        rec->states.push_back(std::move(sr));
+    }
+    struct LagOff { // record mode keeps the three-pass form: its basis is explicit
+        bool &lag;
+        bool saved;
+        LagOff(bool &l, bool off) : lag(l), saved(l) {
+            if (off)
+                lag = false;
+        }
+        ~LagOff() {
+            lag = saved;
+        }
+    };
+
     // Inner GMRES loop driven from the host in batches of speculative steps (steps after the
     // solve ends are no-ops gated on ctl->active).
     void gmres_loop(cudaStream_t st, bool accept_every, int *pinned) {
         (void)accept_every;
+        if (rec) {
+            gmres_loop_record(st, pinned);
+            return;
+        }
         pinned_host = pinned + 1;
         const int batch = 8;
         host_k = 0;
@@ -1447,10 +1552,23 @@ template <class T, class TO> struct IrEngine {
         h.inner_scale = 1.0;
         h.nrows = n;
         h.accept_every = s.accept_every ? 1 : 0;
+        if (s.record) { // the step records carry each step's estimate, check and trigger
+            SolveSettings hs = s;
+            hs.outer_cap = 0;
+            hs.history = true;
+            arm_history(h, hs);
+        }
+        arm_record(h, s);
+        LagOff lag_off(lag, rec != nullptr);
         SPAI_CUDA(cudaMemcpyAsync(ctl, &h, sizeof(Ctl), cudaMemcpyHostToDevice, st));
         SPAI_CUDA(cudaMemsetAsync(counters, 0, 16 * sizeof(int), st));
         gmres_start(st, s.accept_every);
+        if (rec)
+            record_inner_begin(st);
         gmres_loop(st, s.accept_every, pinned);
+        if (rec)
+            record_inner_end(st);
+        rec = nullptr;
     }
 
     // Full refinement solve; b, x are device vectors in TO.
@@ -1471,9 +1589,11 @@ template <class T, class TO> struct IrEngine {
         h.accept_every = s.accept_every ? 1 : 0;
         h.accept_partial = s.restart_at_cap ? 1 : 0;
         arm_history(h, s);
+        arm_record(h, s);
+        LagOff lag_off(lag, rec != nullptr);
         SPAI_CUDA(cudaMemcpyAsync(ctl, &h, sizeof(Ctl), cudaMemcpyHostToDevice, st));
         SPAI_CUDA(cudaMemsetAsync(counters, 0, 16 * sizeof(int), st));
-        if (s.use_graph && !(prof && prof->on)) {
+        if (s.use_graph && !(prof && prof->on) && !rec) {
             if (!exec || graph_f32_accept != s.accept_every)
                 build_graph(st, s.accept_every);
             SPAI_CUDA(cudaMemcpyAsync(bbuf, b, sizeof(TO) * n, cudaMemcpyDeviceToDevice, st));
@@ -1489,13 +1609,20 @@ template <class T, class TO> struct IrEngine {
         SPAI_LAUNCH("ir_x0_kernel");
         residual(st, b, x);
         launches += 2;
+        if (rec)
+            record_state(st, x);
+        int applied = 0;
         for (int step = 0; step <= s.outer_cap; ++step) {
             if (!read_flag(st, pinned, &ctl->outer_active))
                 break;
             make_rhs_kernel<TO, T><<<nblk_vec, kBlock, 0, st>>>(n, r, rhs, ctl);
             SPAI_LAUNCH("make_rhs_kernel");
             gmres_start(st, s.accept_every);
+            if (rec)
+                record_inner_begin(st);
             gmres_loop(st, s.accept_every, pinned);
+            if (rec)
+                record_inner_end(st);
             ir_after_inner_kernel<<<1, 32, 0, st>>>(ctl);
             SPAI_LAUNCH("ir_after_inner_kernel");
             ir_update_kernel<TO, T><<<nblk_vec, kBlock, 0, st>>>(n, x, xn, cand, ctl);
@@ -1506,7 +1633,16 @@ template <class T, class TO> struct IrEngine {
             ir_commit_kernel<TO><<<nblk_vec, kBlock, 0, st>>>(n, x, xn, ctl);
             SPAI_LAUNCH("ir_commit_kernel");
             launches += 5;
+            if (rec) {
+                const Ctl c = fetch_ctl(st);
+                if (c.outer_steps > applied && c.ir_status != 6) { // a correction was applied
+                    applied = c.outer_steps;
+                    rec->inner.back().applied = 1;
+                    record_state(st, x);
+                }
+            }
         }
+        rec = nullptr;
     }
 
     void residual(cudaStream_t st, const TO *b, TO *x) {

@@ -251,6 +251,24 @@ __device__ __forceinline__ int lower_bound_int(const int *a, int n, int v) {
     return lo;
 }
 
+// Record of every fit (the per-fit history of the reference's SpaiColumn,
+// include/bspai/spai.hpp:37-55) for diagnostics on small systems: two append-only streams, ints
+// and binary64 values, written by the column kernel when `ints` is set. Every record starts with
+// 8 ints: kind, column k, workspace tier, fit ordinal (0-based), a, b, c, offset of its values.
+//   kind 1 (fit):    a = |J|, b = |I|; ints J, I; values residual, pivot ratio, coefficients (|J|)
+//   kind 2 (scores): a = candidates, b = selected, c = room for the selection; ints candidates (in
+//                    the fit's order: ascending in exact mode), selected (selection order, b used);
+//                    values mean score, scores (one per candidate)
+// A column refitted from scratch in a larger tier logs again with the higher tier number; records
+// of earlier tiers belong to abandoned attempts.
+struct FitLog {
+    int *ints;
+    double *vals;
+    unsigned long long *top; // [0] ints, [1] values appended (may exceed the capacities)
+    long long int_cap, val_cap;
+    int tier;
+};
+
 template <class T> struct ColumnArgs {
     int n;
     const int *rp, *ci;
@@ -271,7 +289,18 @@ template <class T> struct ColumnArgs {
     int *error;        // bit0 packed output full, bit1 column exceeded the largest workspace
     unsigned long long *phase; // optional cycle counters per fit phase (tuning aid), nullptr = off
     int dyn_scores;            // hand candidates out dynamically (heavy-tailed row lengths)
+    FitLog log;                // optional record of every fit (ints == nullptr: off)
 };
+
+// Appends one record to the fit log (lane 0): reserves `nints` ints (header included) and `nvals`
+// values; io / vo are their offsets, -1 when the log is full (the host sees top > capacity).
+__device__ __forceinline__ void fit_log_reserve(const FitLog &L, int nints, int nvals, long long &io,
+                                                long long &vo) {
+    io = static_cast<long long>(atomicAdd(&L.top[0], static_cast<unsigned long long>(nints)));
+    vo = static_cast<long long>(atomicAdd(&L.top[1], static_cast<unsigned long long>(nvals)));
+    if (io + nints > L.int_cap || vo + nvals > L.val_cap)
+        io = vo = -1;
+}
 
 // Cycle accounting of a fit by phase (lane 0's clock; only when ColumnArgs::phase is set).
 enum FitPhase : int {
@@ -642,6 +671,29 @@ __device__ int fit_column(const Grp &g, const ColumnArgs<T> &A, int k, char *ws,
             lastC[t] = coef[t];
         }
         g.sync();
+        if (A.log.ints) {
+            long long io = 0, vo = 0;
+            if (lane == 0) {
+                fit_log_reserve(A.log, 8 + q + m, 2 + q, io, vo);
+                if (io >= 0) {
+                    int *h = A.log.ints + io;
+                    h[0] = 1, h[1] = k, h[2] = A.log.tier, h[3] = fits - 1;
+                    h[4] = q, h[5] = m, h[6] = 0, h[7] = static_cast<int>(vo);
+                    A.log.vals[vo] = static_cast<double>(res);
+                    A.log.vals[vo + 1] = static_cast<double>(pivot_ratio);
+                }
+            }
+            io = g.shfl(io, 0);
+            vo = g.shfl(vo, 0);
+            if (io >= 0) {
+                for (int t = lane; t < q; t += GS) {
+                    A.log.ints[io + 8 + t] = lastJ[t];
+                    A.log.vals[vo + 2 + t] = static_cast<double>(lastC[t]);
+                }
+                for (int t = lane; t < m; t += GS)
+                    A.log.ints[io + 8 + q + t] = I[t];
+            }
+        }
         if (res <= eps) {
             status = kSuccess;
             break;
@@ -850,6 +902,27 @@ __device__ int fit_column(const Grp &g, const ColumnArgs<T> &A, int k, char *ws,
             status = kNumericalFailure;
             break;
         }
+        long long log_io = -1;
+        if (A.log.ints) {
+            long long vo = 0;
+            if (lane == 0) {
+                fit_log_reserve(A.log, 8 + c + nsel_cap, 1 + c, log_io, vo);
+                if (log_io >= 0) {
+                    int *h = A.log.ints + log_io;
+                    h[0] = 2, h[1] = k, h[2] = A.log.tier, h[3] = fits - 1;
+                    h[4] = c, h[5] = 0, h[6] = nsel_cap, h[7] = static_cast<int>(vo);
+                    A.log.vals[vo] = static_cast<double>(mean);
+                }
+            }
+            log_io = g.shfl(log_io, 0);
+            vo = g.shfl(vo, 0);
+            if (log_io >= 0)
+                for (int t = lane; t < c; t += GS) {
+                    A.log.ints[log_io + 8 + t] = C[t];
+                    A.log.vals[vo + 1 + t] = static_cast<double>(sc[t]);
+                }
+            g.sync();
+        }
         // ---- selection: up to beta smallest (score, index) with score <= mean ----
         int nsel = 0;
         for (; nsel < nsel_cap; ++nsel) {
@@ -883,6 +956,11 @@ __device__ int fit_column(const Grp &g, const ColumnArgs<T> &A, int k, char *ws,
                 sc[best_t] = T(INFINITY); // consumed
             }
             g.sync();
+        }
+        if (log_io >= 0 && lane == 0) {
+            A.log.ints[log_io + 5] = nsel;
+            for (int t = 0; t < nsel; ++t)
+                A.log.ints[log_io + 8 + c + t] = sel[t];
         }
         if (nsel == 0) {
             status = kNoGrowth;
@@ -1340,6 +1418,7 @@ void SpaiBuilder<T>::construct(const DeviceCsr<T> &a, const SpaiParams &prm, cud
                 if (global_cols == 0)
                     global_cols = pending;
             }
+            args.log.tier = static_cast<int>(ti_);
             launch_columns<T>(prm.fast, tp_.G, args, io, tp_.ws, tp_.qcap, gws, threads, blocks, sms, st);
             ++out.launches;
             int h_next = 0;
@@ -1357,7 +1436,19 @@ void SpaiBuilder<T>::construct(const DeviceCsr<T> &a, const SpaiParams &prm, cud
             in_list = out_list;
         }
     };
-    const bool want_tune = prm.tune && prm.group_lanes <= 0 && prm.ws_bytes_per_warp <= 0 && prm.first_qcap <= 0;
+    const bool want_tune = prm.tune && !prm.record && prm.group_lanes <= 0 && prm.ws_bytes_per_warp <= 0 &&
+                           prm.first_qcap <= 0;
+    out.log_ints = nullptr;
+    out.log_vals = nullptr;
+    out.log_top = nullptr;
+    out.log_int_cap = out.log_val_cap = 0;
+    if (prm.record) {
+        const long long want = std::min<long long>(1LL << 28, std::max<long long>(1LL << 20, 64LL * (n + nnz)));
+        out.log_int_cap = out.log_val_cap = want;
+        out.log_ints = arena.alloc<int>(want);
+        out.log_vals = arena.alloc<double>(want);
+        out.log_top = arena.alloc<unsigned long long>(2);
+    }
     for (int attempt = 0;; ++attempt) {
         pidx = arena.alloc<int>(cap);
         pv = arena.alloc<T>(cap);
@@ -1372,6 +1463,8 @@ void SpaiBuilder<T>::construct(const DeviceCsr<T> &a, const SpaiParams &prm, cud
         ColumnArgs<T> args{n, a.rp, a.ci, a.val, tp, ti, d, static_cast<T>(prm.epsilon), prm.alpha,
                            prm.beta, out.col_status, out.col_fits, out.col_growths, out.col_clamps,
                            out.col_q, out.col_residual, off, pidx, pv, top, cap, err, phase, heavy ? 1 : 0};
+        if (out.log_top)
+            SPAI_CUDA(cudaMemsetAsync(out.log_top, 0, 2 * sizeof(unsigned long long), st));
         if (attempt == 0 && want_tune) {
             const TuneChoice c = tune_first_tier<T>(a, prm, heavy, G_def, ws_def, max_threads, smem_budget, sms, st,
                                                     args, queue, err, top, trace, run_chain);
@@ -1383,6 +1476,7 @@ void SpaiBuilder<T>::construct(const DeviceCsr<T> &a, const SpaiParams &prm, cud
                 out.tune_default_ms = c.default_ms;
             }
         }
+        args.log = FitLog{out.log_ints, out.log_vals, out.log_top, out.log_int_cap, out.log_val_cap, 0};
         const std::vector<TierPlan> tiers = plan_tiers(ws0, G0, max_threads, smem_budget, prm.first_qcap, sizeof(T));
         out.group_lanes = tiers[0].G;
         out.ws_bytes = static_cast<int>(tiers[0].ws);

@@ -76,6 +76,7 @@ struct SpaiParams {
     size_t overflow_ws_bytes = 0;
     int first_qcap = 0;          // pattern capacity of the first workspace tier; 0 = by size
     bool tune = true;            // time first-tier candidates on a column sample (large n)
+    bool record = false;         // log every fit (diagnostics; no tuning then)
 };
 
 template <class T> struct SpaiOutput {
@@ -90,6 +91,11 @@ template <class T> struct SpaiOutput {
     double tune_sample_ms = 0, tune_default_ms = 0; // chosen / default pair's time on the sample
     int overflow_columns_global = 0;
     T *d = nullptr;
+    // Fit log of a recording build (device streams and their appended counts, see FitLog).
+    int *log_ints = nullptr;
+    double *log_vals = nullptr;
+    unsigned long long *log_top = nullptr;
+    long long log_int_cap = 0, log_val_cap = 0;
     int *col_status = nullptr, *col_fits = nullptr, *col_growths = nullptr, *col_clamps = nullptr,
         *col_q = nullptr;
     T *col_residual = nullptr;

@@ -68,11 +68,11 @@ class InnerRecord(ctypes.Structure):
 
 class IterationRecord(ctypes.Structure):
     _fields_ = [("inner", ctypes.c_int64), ("iteration", ctypes.c_int64), ("estimated_relative", ctypes.c_double),
-                ("recomputed_relative", ctypes.c_double), ("accepted", ctypes.c_int32), ("pad", ctypes.c_int32)]
+                ("recomputed_relative", ctypes.c_double), ("accepted", ctypes.c_int32), ("triggered", ctypes.c_int32)]
 
 
 def _records(arr, count):
-    return [{f: getattr(arr[i], f) for f, _ in arr[i]._fields_ if f != "pad"} for i in range(count)]
+    return [{f: getattr(arr[i], f) for f, _ in arr[i]._fields_ } for i in range(count)]
 
 
 class Report(ctypes.Structure):
@@ -134,6 +134,12 @@ SIGNATURES = {
     "spai_backward_error_noalloc": (ctypes.c_int, [VP, VP, VP, VP, VP]),
     "spai_tuning": (ctypes.c_int, [VP, I32P, F64P]),
     "spai_hypot_device": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int64, F64P, F64P, F64P]),
+    "spai_set_preconditioner": (ctypes.c_int, [VP, ctypes.POINTER(Csr)]),
+    "spai_record": (ctypes.c_int, [VP, ctypes.c_int32]),
+    "spai_fit_log": (ctypes.c_int, [VP, I32P, ctypes.c_int64, I64P, F64P, ctypes.c_int64, I64P]),
+    "spai_record_counts": (ctypes.c_int, [VP, I64P, I64P]),
+    "spai_record_state": (ctypes.c_int, [VP, ctypes.c_int64, F64P, F64P]),
+    "spai_record_inner": (ctypes.c_int, [VP, ctypes.c_int64, F64P, F64P, F64P, F64P, F64P, F64P, F64P]),
     "spai_hypot": (ctypes.c_double, [ctypes.c_double, ctypes.c_double]),
     "spai_hypotf": (ctypes.c_float, [ctypes.c_float, ctypes.c_float]),
 }
@@ -276,6 +282,84 @@ class Handle:
         _check(lib().spai_gmres(self._h, _p(rhs, F64P), _p(x, F64P), tau, cap, ctypes.byref(st),
                                 ctypes.byref(it), ctypes.byref(rel)))
         return x, dict(status=st.value, iterations=it.value, final_relative=rel.value)
+
+    def set_preconditioner(self, p):
+        """Solve with a caller-supplied preconditioner P (canonical CSR (n, ptr, idx, val))."""
+        self._p = _CsrHolder(p)
+        _check(lib().spai_set_preconditioner(self._h, ctypes.byref(self._p.csr)))
+
+    def record(self, enable=True):
+        """Record mode (binary64): fit log of the next build, every step of the next solves."""
+        _check(lib().spai_record(self._h, 1 if enable else 0))
+
+    def fit_log(self):
+        """Fit histories of the last recorded build: {column: [fit dict, ...]} in fit order.
+
+        Each fit: J, I (index lists), coefficients, residual, pivot_ratio and, for fits that
+        went on to candidate scoring, candidates, scores, mean_score, selected (selection
+        order). Records of abandoned workspace tiers are dropped (the column's highest tier
+        holds its history)."""
+        ni, nv = ctypes.c_int64(), ctypes.c_int64()
+        _check(lib().spai_fit_log(self._h, None, 0, ctypes.byref(ni), None, 0, ctypes.byref(nv)))
+        ints = np.zeros(max(ni.value, 1), np.int32)
+        vals = np.zeros(max(nv.value, 1))
+        _check(lib().spai_fit_log(self._h, _p(ints, I32P), ni.value, ctypes.byref(ni), _p(vals, F64P), nv.value,
+                                  ctypes.byref(nv)))
+        recs = {}
+        pos = 0
+        while pos < ni.value:
+            kind, k, tier, fit, a, b, c, vo = (int(v) for v in ints[pos:pos + 8])
+            body = ints[pos + 8:]
+            if kind == 1:
+                rec = dict(J=body[:a].tolist(), I=body[a:a + b].tolist(), residual=float(vals[vo]),
+                           pivot_ratio=float(vals[vo + 1]), coefficients=vals[vo + 2:vo + 2 + a].copy())
+                pos += 8 + a + b
+            elif kind == 2:
+                rec = dict(candidates=body[:a].tolist(), selected=body[a:a + b].tolist(),
+                           mean_score=float(vals[vo]), scores=vals[vo + 1:vo + 1 + a].copy())
+                pos += 8 + a + c
+            else:
+                raise SpaiError(-1, f"corrupt fit log record kind {kind} at {pos}")
+            recs.setdefault(k, []).append((tier, fit, kind, rec))
+        out = {}
+        for k, lst in recs.items():
+            top = max(t for t, _, _, _ in lst)
+            fits = {}
+            for tier, fit, kind, rec in lst:
+                if tier == top:
+                    fits.setdefault(fit, {}).update(rec)
+            out[k] = [fits[f] for f in sorted(fits)]
+        return out
+
+    def recorded(self):
+        """Record of the last recorded solve: dict(states=[(x, residual)], inner=[dict])."""
+        L = lib()
+        ns, nin = ctypes.c_int64(), ctypes.c_int64()
+        _check(L.spai_record_counts(self._h, ctypes.byref(ns), ctypes.byref(nin)))
+        n = self.n
+        states = []
+        for s in range(ns.value):
+            x, r = np.zeros(n), np.zeros(n)
+            _check(L.spai_record_state(self._h, s, _p(x, F64P), _p(r, F64P)))
+            states.append((x, r))
+        inner = []
+        for i in range(nin.value):
+            sm = np.zeros(12)
+            _check(L.spai_record_inner(self._h, i, _p(sm, F64P), None, None, None, None, None, None))
+            m, nb, hr, hc = int(sm[2]), int(sm[8]), int(sm[9]), int(sm[10])
+            rhs, sol = np.zeros(n), np.zeros(n)
+            basis = np.zeros((max(nb, 1), n))
+            hess = np.zeros((max(hr, 1), max(hc, 1)))
+            steps = np.zeros((max(m, 1), 8))
+            cands = np.zeros((max(m, 1), n))
+            _check(L.spai_record_inner(self._h, i, _p(sm, F64P), _p(rhs, F64P), _p(sol, F64P), _p(basis, F64P),
+                                       _p(hess, F64P), _p(steps, F64P), _p(cands, F64P)))
+            inner.append(dict(status=int(sm[0]), converged=bool(sm[1]), steps=m, applied=bool(sm[3]),
+                              initial_original=float(sm[4]), initial_preconditioned=float(sm[5]),
+                              final_original=float(sm[6]), final_preconditioned=float(sm[7]),
+                              iterations=int(sm[11]), rhs=rhs, solution=sol, basis=basis[:nb],
+                              hessenberg=hess[:hr, :hc], step_rows=steps[:m], candidates=cands[:m]))
+        return dict(states=states, inner=inner)
 
     def backward_error_noalloc(self, d_b, d_x, d_out, stream=None):
         """Allocation-free backward error of device vector x (see spai_backward_error_noalloc)."""

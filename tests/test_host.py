@@ -2,6 +2,7 @@
 the host build of the device hypot agrees with the oracle, the drop-in CLIs' input-error exit
 codes (tests/check_solver_cli.py cases that fail before any device work), the seeded generators,
 and the replica reduction of bench.py over a world_size-2 gloo group."""
+import math
 import os
 import re
 import subprocess
@@ -272,3 +273,26 @@ def test_mm_reader_host_path_invalid_entries_and_edge_cases(built, tmp_path):
     p.write_text("%%MatrixMarket matrix coordinate integer general\n2 2 3\n2 2 +7\n1 2 -3\n2 2 -07\n")
     (n, ptr, idx, val), cols, _ = spai_ir.mm_read(p, 1 << 62)
     assert ptr.tolist() == [0, 1, 1] and idx.tolist() == [1] and val.tolist() == [-3.0]
+
+
+def test_snapshot_number_format_round_trips():
+    """The release snapshot's numbers: C99 hex-float plus '@' and the IEEE-754 bits
+    (tests/release_cpu_snapshot.cpp:38-57 of the reference), exact for every finite binary64."""
+    import struct
+
+    from spai_ir import snapshot as S
+
+    rng = np.random.default_rng(11)
+    values = [0.0, -0.0, 1.0, -1.5, 0.1, 5e-324, 2.2250738585072014e-308, 1.7976931348623157e308,
+              math.ldexp(1.0, -1074), -math.ldexp(3.0, -1060)] + list(rng.standard_normal(200) * 10.0 ** rng.integers(-300, 300, 200))
+    for v in values:
+        text = S._hex(v)
+        lit, bits = text.split("@")
+        x = float.fromhex(lit)
+        assert struct.pack(">d", x) == struct.pack(">d", v), text
+        assert struct.unpack(">Q", struct.pack(">d", x))[0] == int(bits, 16)
+    for bad in (math.inf, -math.inf, math.nan):
+        with pytest.raises(ValueError):
+            S._hex(bad)
+    assert S._hex(1.0) == "0x1.0000000000000p0@3ff0000000000000"
+    assert S._hex(-0.0) == "-0x0.0000000000000p-1022@8000000000000000"
