@@ -236,8 +236,8 @@ int spai_record(spai_handle *h, int32_t enable);
 /* Fit log of the last build in record mode: an int stream and a binary64 stream of records, each
  * with an 8-int header (kind, column, workspace tier, fit ordinal, a, b, c, offset of its values):
  * kind 1 (fit): a = |J|, b = |I|; ints J then I; values residual, pivot ratio, coefficients;
- * kind 2 (candidate scores): a = candidates, b = selected, c = room; ints candidates then the
- * selection (in selection order, b used of c); values mean score, then one score per candidate.
+ * kind 2 (candidate scores): a = candidates; ints candidates; values mean score, then one score
+ * per candidate; kind 3 (selection): a = selected; ints the selection in selection order.
  * A column refitted from scratch in a larger workspace tier logs again under the higher tier;
  * only its highest tier's records are its history. n_ints / n_vals give the stream lengths;
  * SPAI_ERR_WORKSPACE when the log overflowed. */

@@ -36,15 +36,54 @@ __global__ void convert_kernel(long long count, const TS *src, TD *dst) {
         dst[i] = static_cast<TD>(src[i]);
 }
 
+// Device form of the canonical CSR check below, fused with the int64 -> int32 narrowing of the
+// upload: offsets within [0, nnz] and nondecreasing, columns in range and strictly increasing per
+// row, values finite and nonzero. Offsets are clamped into [0, nnz] before use and a row whose
+// offsets decrease is skipped, so no read leaves the arrays whatever the input; *bad != 0 means
+// canonical_error (host) names the first violation.
+__global__ void csr_offsets_kernel(long long n, long long nnz, const long long *rp64, int *rp32, int *bad) {
+    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i <= n;
+         i += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const long long v = rp64[i];
+        if (v < 0 || v > nnz || (i < n && rp64[i + 1] < v))
+            *bad = 1;
+        rp32[i] = static_cast<int>(v < 0 ? 0 : (v > nnz ? nnz : v));
+    }
+}
+__global__ void csr_entries_kernel(int n, const int *rp32, const long long *ci64, const double *val, int *ci32,
+                                   int *bad) {
+    int flag = 0;
+    for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < n; row += gridDim.x * blockDim.x) {
+        const int b = rp32[row], e = rp32[row + 1];
+        long long prev = -1;
+        for (int t = b; t < e; ++t) {
+            const long long c = ci64[t];
+            const double v = val[t];
+            flag |= c < 0 || c >= n || c <= prev || !isfinite(v) || v == 0.0;
+            ci32[t] = static_cast<int>(c < 0 || c >= n ? 0 : c);
+            prev = c;
+        }
+    }
+    if (flag)
+        *bad = 1;
+}
+
 // Canonical CSR check (src/cuda_spai.cu:452-470): offsets monotone from 0 to nnz, columns in
 // range and strictly increasing per row, values finite and nonzero.
-std::string canonical_error(const spai_csr *a) {
+// The O(1) part: pointers, sizes, first and last offset (checked before any upload).
+std::string canonical_header_error(const spai_csr *a) {
     if (!a || a->n <= 0 || a->nnz < 0 || !a->row_offsets || (a->nnz > 0 && (!a->col_indices || !a->values)))
         return "CSR pointers/sizes invalid";
     if (a->n > INT_MAX - 1 || a->nnz > INT_MAX - 1)
         return "matrix exceeds 32-bit device index range";
     if (a->row_offsets[0] != 0 || a->row_offsets[a->n] != a->nnz)
         return "row offsets must run from 0 to nnz";
+    return "";
+}
+std::string canonical_error(const spai_csr *a) {
+    const std::string head = canonical_header_error(a);
+    if (!head.empty())
+        return head;
     for (int64_t r = 0; r < a->n; ++r) {
         const int64_t b = a->row_offsets[r], e = a->row_offsets[r + 1];
         if (b > e)
@@ -437,9 +476,11 @@ int adjoint_device_impl(spai_handle *h, int nrhs, const double *d_x, const doubl
 } // namespace spai_api
 
 namespace spai_api {
-// Canonical host CSR -> device CSR in `dst` (64-bit indices narrowed on the device through the
-// handle's scratch arena); stream-ordered.
-DeviceCsr<double> upload_csr(spai_handle *h, DeviceArena &dst, const spai_csr *a) {
+// Host CSR -> device CSR in `dst` (64-bit indices narrowed on the device through the handle's
+// scratch arena), checked on the device for the canonical form on the way; stream-ordered. The
+// caller synchronises and, when *bad is set, reports canonical_error's message. `a` must pass
+// canonical_header_error.
+DeviceCsr<double> upload_csr(spai_handle *h, DeviceArena &dst, const spai_csr *a, int *bad) {
     const int n = static_cast<int>(a->n), nnz = static_cast<int>(a->nnz);
     DeviceCsr<double> m;
     m.n = n;
@@ -451,20 +492,68 @@ DeviceCsr<double> upload_csr(spai_handle *h, DeviceArena &dst, const spai_csr *a
     m.rp = dst.alloc<int>(n + 1);
     m.ci = dst.alloc<int>(nnz > 0 ? nnz : 1);
     m.val = dst.alloc<double>(nnz > 0 ? nnz : 1);
-    h->scratch.reset();
     long long *tmp = h->scratch.alloc<long long>(std::max(n + 1, nnz));
     cudaStream_t st = h->stream;
+    SPAI_CUDA(cudaMemsetAsync(bad, 0, sizeof(int), st));
     SPAI_CUDA(cudaMemcpyAsync(tmp, a->row_offsets, sizeof(long long) * (n + 1), cudaMemcpyHostToDevice, st));
-    narrow_kernel<<<grid_for(n + 1, 256, h->sms * 8), 256, 0, st>>>(n + 1, tmp, m.rp);
-    SPAI_LAUNCH("narrow_kernel");
+    csr_offsets_kernel<<<grid_for(n + 1, 256, h->sms * 8), 256, 0, st>>>(n, nnz, tmp, m.rp, bad);
+    SPAI_LAUNCH("csr_offsets_kernel");
     if (nnz > 0) {
         // The index copy reuses tmp after the row offsets are narrowed (stream order).
-        SPAI_CUDA(cudaMemcpyAsync(tmp, a->col_indices, sizeof(long long) * nnz, cudaMemcpyHostToDevice, st));
-        narrow_kernel<<<grid_for(nnz, 256, h->sms * 8), 256, 0, st>>>(nnz, tmp, m.ci);
-        SPAI_LAUNCH("narrow_kernel");
         SPAI_CUDA(cudaMemcpyAsync(m.val, a->values, sizeof(double) * nnz, cudaMemcpyHostToDevice, st));
+        SPAI_CUDA(cudaMemcpyAsync(tmp, a->col_indices, sizeof(long long) * nnz, cudaMemcpyHostToDevice, st));
+        csr_entries_kernel<<<grid_for(n, 256, h->sms * 8), 256, 0, st>>>(n, m.rp, tmp, m.val, m.ci, bad);
+        SPAI_LAUNCH("csr_entries_kernel");
     }
     return m;
+}
+} // namespace spai_api
+
+namespace spai_api {
+// Branch-free scans (the compiler vectorises them): an exponent field of all ones is Inf or NaN.
+bool all_finite(int64_t n, const double *v) {
+    uint64_t bad = 0;
+    for (int64_t i = 0; i < n; ++i) {
+        uint64_t u;
+        std::memcpy(&u, v + i, sizeof u);
+        bad |= static_cast<uint64_t>(((u >> 52) & 0x7ff) == 0x7ff);
+    }
+    return bad == 0;
+}
+bool finite_inputs(int64_t n, const double *b, const double *reference) {
+    return all_finite(n, b) && (!reference || all_finite(n, reference));
+}
+// spai_solve once b and reference are known to be finite.
+int solve_host_impl(spai_handle *h, const double *b, double *x, const double *reference,
+                    const spai_options *opt, spai_report *rep) {
+    API_BEGIN
+    const int n = h->n;
+    h->scratch.reset();
+    double *db = h->scratch.alloc<double>(n);
+    double *dx = h->scratch.alloc<double>(n);
+    SPAI_CUDA(cudaMemcpyAsync(db, b, sizeof(double) * n, cudaMemcpyHostToDevice, h->stream));
+    const int rc = solve_device_impl(h, db, dx, *opt, rep);
+    if (rc != SPAI_OK)
+        return rc;
+    if (rep->ir_status != IR_CONSTRUCTION_FAILURE && rep->ir_status != IR_INVALID_INPUT) {
+        SPAI_CUDA(cudaMemcpyAsync(x, dx, sizeof(double) * n, cudaMemcpyDeviceToHost, h->stream));
+        SPAI_CUDA(cudaStreamSynchronize(h->stream));
+        if (reference) {
+            double rinf = 0, einf = 0;
+            bool overflow = false;
+            for (int i = 0; i < n; ++i) {
+                rinf = std::max(rinf, std::fabs(reference[i]));
+                const double e = std::fabs(x[i] - reference[i]);
+                overflow |= !std::isfinite(e);
+                einf = std::max(einf, e);
+            }
+            rep->forward_error = rinf == 0 ? einf : einf / rinf;
+            if (overflow || !std::isfinite(rep->forward_error))
+                rep->forward_error = INFINITY;
+        }
+    }
+    return SPAI_OK;
+    API_END
 }
 } // namespace spai_api
 
@@ -507,7 +596,7 @@ int spai_create(const spai_csr *a, int32_t precision, int device, void *stream, 
     if (!out || precision < 0 || precision > 2)
         return fail(SPAI_ERR_ARGUMENT, "spai_create: bad arguments");
     *out = nullptr;
-    const std::string why = canonical_error(a);
+    const std::string why = canonical_header_error(a);
     if (!why.empty())
         return fail(SPAI_ERR_ARGUMENT, "spai_create: " + why);
     SPAI_CUDA(cudaSetDevice(device));
@@ -526,7 +615,9 @@ int spai_create(const spai_csr *a, int32_t precision, int device, void *stream, 
     SPAI_CUDA(cudaMallocHost(&h->pinned, 64));
     const int n = h->n, nnz = h->nnz;
     cudaStream_t st = h->stream;
-    h->a64 = upload_csr(h.get(), h->mat, a);
+    h->scratch.reset();
+    int *bad = h->scratch.alloc<int>(1);
+    h->a64 = upload_csr(h.get(), h->mat, a, bad);
     if (precision != SPAI_PREC_F64) {
         h->a32.n = n;
         h->a32.nnz = nnz;
@@ -537,7 +628,13 @@ int spai_create(const spai_csr *a, int32_t precision, int device, void *stream, 
         convert_kernel<float, double><<<grid_for(nnz, 256, h->sms * 8), 256, 0, st>>>(nnz, h->a64.val, h->a32.val);
         SPAI_LAUNCH("convert_kernel");
     }
+    int h_bad = 0;
+    SPAI_CUDA(cudaMemcpyAsync(&h_bad, bad, sizeof(int), cudaMemcpyDeviceToHost, st));
     SPAI_CUDA(cudaStreamSynchronize(st));
+    if (h_bad) { // the host check names the first violation
+        const std::string full = canonical_error(a);
+        return fail(SPAI_ERR_ARGUMENT, "spai_create: " + (full.empty() ? std::string("CSR is not canonical") : full));
+    }
     *out = h.release();
     return SPAI_OK;
     API_END
@@ -639,6 +736,7 @@ int spai_solve_device(spai_handle *h, const double *d_b, double *d_x, const spai
     API_END
 }
 
+
 int spai_solve(spai_handle *h, const double *b, double *x, const double *reference,
                const spai_options *opt, spai_report *rep) {
     API_BEGIN
@@ -649,40 +747,15 @@ int spai_solve(spai_handle *h, const double *b, double *x, const double *referen
         rep = &local;
     clear_report(rep);
     SPAI_CUDA(cudaSetDevice(h->device));
-    const int n = h->n;
-    for (int i = 0; i < n; ++i)
-        if (!std::isfinite(b[i]) || (reference && !std::isfinite(reference[i]))) {
-            rep->ir_status = IR_INVALID_INPUT; // src/ir.cpp:48-53
-            rep->spai_status = h->spai_status;
-            return SPAI_OK;
-        }
-    h->scratch.reset();
-    double *db = h->scratch.alloc<double>(n);
-    double *dx = h->scratch.alloc<double>(n);
-    SPAI_CUDA(cudaMemcpyAsync(db, b, sizeof(double) * n, cudaMemcpyHostToDevice, h->stream));
-    const int rc = solve_device_impl(h, db, dx, *opt, rep);
-    if (rc != SPAI_OK)
-        return rc;
-    if (rep->ir_status != IR_CONSTRUCTION_FAILURE && rep->ir_status != IR_INVALID_INPUT) {
-        SPAI_CUDA(cudaMemcpyAsync(x, dx, sizeof(double) * n, cudaMemcpyDeviceToHost, h->stream));
-        SPAI_CUDA(cudaStreamSynchronize(h->stream));
-        if (reference) {
-            double rinf = 0, einf = 0;
-            bool overflow = false;
-            for (int i = 0; i < n; ++i) {
-                rinf = std::max(rinf, std::fabs(reference[i]));
-                const double e = std::fabs(x[i] - reference[i]);
-                overflow |= !std::isfinite(e);
-                einf = std::max(einf, e);
-            }
-            rep->forward_error = rinf == 0 ? einf : einf / rinf;
-            if (overflow || !std::isfinite(rep->forward_error))
-                rep->forward_error = INFINITY;
-        }
+    if (!finite_inputs(h->n, b, reference)) {
+        rep->ir_status = IR_INVALID_INPUT; // src/ir.cpp:48-53
+        rep->spai_status = h->spai_status;
+        return SPAI_OK;
     }
-    return SPAI_OK;
+    return solve_host_impl(h, b, x, reference, opt, rep);
     API_END
 }
+
 
 int spai_ir_solve(const spai_csr *a, const double *b, double *x, const double *reference,
                   const spai_options *opt, spai_report *rep, void *stream) {
@@ -702,16 +775,16 @@ int spai_ir_solve(const spai_csr *a, const double *b, double *x, const double *r
         rep->ir_status = IR_INVALID_INPUT;
         return SPAI_OK;
     }
-    for (int64_t i = 0; i < a->n; ++i)
-        if (!std::isfinite(b[i]) || (reference && !std::isfinite(reference[i]))) {
-            rep->ir_status = IR_INVALID_INPUT;
-            return SPAI_OK;
-        }
+    if (!finite_inputs(a->n, b, reference)) {
+        rep->ir_status = IR_INVALID_INPUT;
+        return SPAI_OK;
+    }
     spai_report brep;
     rc = spai_build(h, opt, &brep);
     if (rc != SPAI_OK)
         return rc;
-    rc = spai_solve(h, b, x, reference, opt, rep);
+    clear_report(rep);
+    rc = solve_host_impl(h, b, x, reference, opt, rep);
     rep->spai_fits = brep.spai_fits;
     rep->spai_growths = brep.spai_growths;
     rep->spai_overflow_columns = brep.spai_overflow_columns;
@@ -990,7 +1063,7 @@ int spai_set_preconditioner(spai_handle *h, const spai_csr *p) {
     API_BEGIN
     if (!h || !p)
         return fail(SPAI_ERR_ARGUMENT, "spai_set_preconditioner: null argument");
-    const std::string why = canonical_error(p);
+    const std::string why = canonical_header_error(p);
     if (!why.empty())
         return fail(SPAI_ERR_ARGUMENT, "spai_set_preconditioner: " + why);
     if (p->n != h->n)
@@ -1002,7 +1075,16 @@ int spai_set_preconditioner(spai_handle *h, const spai_csr *p) {
     h->adj_ready = false;
     h->adj_cap = -1;
     h->build.reset();
-    const DeviceCsr<double> p64 = upload_csr(h, h->build, p);
+    h->scratch.reset();
+    int *bad = h->scratch.alloc<int>(1);
+    const DeviceCsr<double> p64 = upload_csr(h, h->build, p, bad);
+    int h_bad = 0;
+    SPAI_CUDA(cudaMemcpyAsync(&h_bad, bad, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    SPAI_CUDA(cudaStreamSynchronize(h->stream));
+    if (h_bad) {
+        const std::string full = canonical_error(p);
+        return fail(SPAI_ERR_ARGUMENT, "spai_set_preconditioner: " + (full.empty() ? std::string("CSR is not canonical") : full));
+    }
     if (h->precision == SPAI_PREC_F64) {
         h->s64 = SpaiOutput<double>{};
         h->s64.n = h->n;

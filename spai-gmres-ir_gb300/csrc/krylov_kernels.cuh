@@ -1186,6 +1186,10 @@ template <class T, class TO> struct IrEngine {
         {
             size_t free_b = 0, total_b = 0;
             SPAI_CUDA(cudaMemGetInfo(&free_b, &total_b));
+            if (vcount * sizeof(T) > free_b) { // cached blocks of earlier handles count as free
+                block_cache().release();
+                SPAI_CUDA(cudaMemGetInfo(&free_b, &total_b));
+            }
             if (vcount * sizeof(T) > free_b)
                 throw WorkspaceError("Krylov basis of " + std::to_string(cap + 1) + " vectors of " +
                                      std::to_string(n) + " rows needs " +

@@ -256,9 +256,9 @@ __device__ __forceinline__ int lower_bound_int(const int *a, int n, int v) {
 // and binary64 values, written by the column kernel when `ints` is set. Every record starts with
 // 8 ints: kind, column k, workspace tier, fit ordinal (0-based), a, b, c, offset of its values.
 //   kind 1 (fit):    a = |J|, b = |I|; ints J, I; values residual, pivot ratio, coefficients (|J|)
-//   kind 2 (scores): a = candidates, b = selected, c = room for the selection; ints candidates (in
-//                    the fit's order: ascending in exact mode), selected (selection order, b used);
-//                    values mean score, scores (one per candidate)
+//   kind 2 (scores): a = candidates; ints candidates (in the fit's order: ascending in exact
+//                    mode); values mean score, scores (one per candidate)
+//   kind 3 (selection): a = selected; ints the selection in selection order
 // A column refitted from scratch in a larger tier logs again with the higher tier number; records
 // of earlier tiers belong to abandoned attempts.
 struct FitLog {
@@ -550,7 +550,7 @@ __global__ void score_kat_kernel(T rsq, T dot, T den, double *out) {
 
 // One adaptive column (src/spai.cpp:100-244). Returns a final SpaiStatus or kOverflow when the
 // workspace (ws, cap bytes; J capacity qcap) is too small for this column.
-template <bool FAST, class Grp, class T>
+template <bool FAST, bool LOG, class Grp, class T>
 __device__ int fit_column(const Grp &g, const ColumnArgs<T> &A, int k, char *ws, size_t cap, int qcap) {
     const int lane = g.thread_rank();
     constexpr int GS = Grp::size();
@@ -671,7 +671,7 @@ __device__ int fit_column(const Grp &g, const ColumnArgs<T> &A, int k, char *ws,
             lastC[t] = coef[t];
         }
         g.sync();
-        if (A.log.ints) {
+        if (LOG) {
             long long io = 0, vo = 0;
             if (lane == 0) {
                 fit_log_reserve(A.log, 8 + q + m, 2 + q, io, vo);
@@ -902,23 +902,22 @@ __device__ int fit_column(const Grp &g, const ColumnArgs<T> &A, int k, char *ws,
             status = kNumericalFailure;
             break;
         }
-        long long log_io = -1;
-        if (A.log.ints) {
-            long long vo = 0;
+        if (LOG) {
+            long long io = 0, vo = 0;
             if (lane == 0) {
-                fit_log_reserve(A.log, 8 + c + nsel_cap, 1 + c, log_io, vo);
-                if (log_io >= 0) {
-                    int *h = A.log.ints + log_io;
+                fit_log_reserve(A.log, 8 + c, 1 + c, io, vo);
+                if (io >= 0) {
+                    int *h = A.log.ints + io;
                     h[0] = 2, h[1] = k, h[2] = A.log.tier, h[3] = fits - 1;
-                    h[4] = c, h[5] = 0, h[6] = nsel_cap, h[7] = static_cast<int>(vo);
+                    h[4] = c, h[5] = 0, h[6] = 0, h[7] = static_cast<int>(vo);
                     A.log.vals[vo] = static_cast<double>(mean);
                 }
             }
-            log_io = g.shfl(log_io, 0);
+            io = g.shfl(io, 0);
             vo = g.shfl(vo, 0);
-            if (log_io >= 0)
+            if (io >= 0)
                 for (int t = lane; t < c; t += GS) {
-                    A.log.ints[log_io + 8 + t] = C[t];
+                    A.log.ints[io + 8 + t] = C[t];
                     A.log.vals[vo + 1 + t] = static_cast<double>(sc[t]);
                 }
             g.sync();
@@ -957,10 +956,16 @@ __device__ int fit_column(const Grp &g, const ColumnArgs<T> &A, int k, char *ws,
             }
             g.sync();
         }
-        if (log_io >= 0 && lane == 0) {
-            A.log.ints[log_io + 5] = nsel;
-            for (int t = 0; t < nsel; ++t)
-                A.log.ints[log_io + 8 + c + t] = sel[t];
+        if (LOG && lane == 0) {
+            long long io = 0, vo = 0;
+            fit_log_reserve(A.log, 8 + nsel, 0, io, vo);
+            if (io >= 0) {
+                int *h = A.log.ints + io;
+                h[0] = 3, h[1] = k, h[2] = A.log.tier, h[3] = fits - 1;
+                h[4] = nsel, h[5] = 0, h[6] = 0, h[7] = static_cast<int>(vo);
+                for (int t = 0; t < nsel; ++t)
+                    h[8 + t] = sel[t];
+            }
         }
         if (nsel == 0) {
             status = kNoGrowth;
@@ -1020,7 +1025,9 @@ __device__ int fit_column(const Grp &g, const ColumnArgs<T> &A, int k, char *ws,
 // Persistent column kernel with G lanes per column (32/G columns per warp): groups take columns
 // from io (all columns, or the previous tier's misfits) with a workspace of ws_bytes per group in
 // shared memory (gws == nullptr) or in global memory (gws + group * ws_bytes).
-template <class T, int G, bool FAST>
+// LOG: the build records every fit (FitLog); a separate instantiation, so the production kernels
+// carry no logging code.
+template <class T, int G, bool FAST, bool LOG>
 __global__ void __launch_bounds__(sizeof(T) == 8 ? 512 : 768)
     spai_columns_kernel(ColumnArgs<T> A, TierIo io, size_t ws_bytes, int qcap, char *gws) {
     extern __shared__ __align__(16) char smem[];
@@ -1038,7 +1045,7 @@ __global__ void __launch_bounds__(sizeof(T) == 8 ? 512 : 768)
         if (slot >= total)
             break;
         const int k = io.in_list ? io.in_list[slot] : slot;
-        const int r = fit_column<FAST>(g, A, k, ws, ws_bytes, qcap);
+        const int r = fit_column<FAST, LOG>(g, A, k, ws, ws_bytes, qcap);
         if (r == kOverflow && lane == 0) {
             if (io.out_list)
                 io.out_list[atomicAdd(io.out_count, 1)] = k;
@@ -1111,47 +1118,49 @@ __global__ void stats_kernel(int n, const int *__restrict__ fits, const int *__r
 // ------------------------------------------------------------------------------------------
 // Launch the column kernel for a group width G with `threads` per block: persistent over the
 // SMs (shared-memory workspace, at most max_blocks blocks) or exactly max_blocks blocks (global).
-template <class T, int G, bool FAST>
+template <class T, int G, bool FAST, bool LOG>
 void launch_columns_g(ColumnArgs<T> args, TierIo io, size_t ws, int qcap, char *gws, int threads,
                       long long max_blocks, int sms, cudaStream_t st) {
     long long blocks = max_blocks;
     size_t smem = 0;
     if (!gws) {
         smem = ws * static_cast<size_t>(threads / G);
-        SPAI_CUDA(cudaFuncSetAttribute(spai_columns_kernel<T, G, FAST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        SPAI_CUDA(cudaFuncSetAttribute(spai_columns_kernel<T, G, FAST, LOG>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        static_cast<int>(smem)));
         int per_sm = 0;
-        SPAI_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, spai_columns_kernel<T, G, FAST>, threads, smem));
+        SPAI_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, spai_columns_kernel<T, G, FAST, LOG>, threads, smem));
         blocks = std::min<long long>(max_blocks, static_cast<long long>(sms) * std::max(per_sm, 1));
     }
-    spai_columns_kernel<T, G, FAST><<<static_cast<unsigned>(std::max<long long>(blocks, 1)), threads, smem, st>>>(
+    spai_columns_kernel<T, G, FAST, LOG><<<static_cast<unsigned>(std::max<long long>(blocks, 1)), threads, smem, st>>>(
         args, io, ws, qcap, gws);
     SPAI_LAUNCH("spai_columns_kernel");
 }
-template <class T, bool FAST>
+template <class T, bool FAST, bool LOG>
 void launch_columns_f(int G, ColumnArgs<T> args, TierIo io, size_t ws, int qcap, char *gws, int threads,
                       long long max_blocks, int sms, cudaStream_t st) {
     switch (G) {
     case 4:
-        launch_columns_g<T, 4, FAST>(args, io, ws, qcap, gws, threads, max_blocks, sms, st);
+        launch_columns_g<T, 4, FAST, LOG>(args, io, ws, qcap, gws, threads, max_blocks, sms, st);
         break;
     case 8:
-        launch_columns_g<T, 8, FAST>(args, io, ws, qcap, gws, threads, max_blocks, sms, st);
+        launch_columns_g<T, 8, FAST, LOG>(args, io, ws, qcap, gws, threads, max_blocks, sms, st);
         break;
     case 16:
-        launch_columns_g<T, 16, FAST>(args, io, ws, qcap, gws, threads, max_blocks, sms, st);
+        launch_columns_g<T, 16, FAST, LOG>(args, io, ws, qcap, gws, threads, max_blocks, sms, st);
         break;
     default:
-        launch_columns_g<T, 32, FAST>(args, io, ws, qcap, gws, threads, max_blocks, sms, st);
+        launch_columns_g<T, 32, FAST, LOG>(args, io, ws, qcap, gws, threads, max_blocks, sms, st);
     }
 }
 template <class T>
 void launch_columns(bool fast, int G, ColumnArgs<T> args, TierIo io, size_t ws, int qcap, char *gws, int threads,
                     long long max_blocks, int sms, cudaStream_t st) {
     if (fast)
-        launch_columns_f<T, true>(G, args, io, ws, qcap, gws, threads, max_blocks, sms, st);
+        launch_columns_f<T, true, false>(G, args, io, ws, qcap, gws, threads, max_blocks, sms, st);
+    else if (args.log.ints)
+        launch_columns_f<T, false, true>(G, args, io, ws, qcap, gws, threads, max_blocks, sms, st);
     else
-        launch_columns_f<T, false>(G, args, io, ws, qcap, gws, threads, max_blocks, sms, st);
+        launch_columns_f<T, false, false>(G, args, io, ws, qcap, gws, threads, max_blocks, sms, st);
 }
 
 // One workspace tier: group width, bytes per group, groups per block, pattern capacity, and
@@ -1442,7 +1451,7 @@ void SpaiBuilder<T>::construct(const DeviceCsr<T> &a, const SpaiParams &prm, cud
     out.log_vals = nullptr;
     out.log_top = nullptr;
     out.log_int_cap = out.log_val_cap = 0;
-    if (prm.record) {
+    if (prm.record && !prm.fast) { // the log follows the exact mode's fits
         const long long want = std::min<long long>(1LL << 28, std::max<long long>(1LL << 20, 64LL * (n + nnz)));
         out.log_int_cap = out.log_val_cap = want;
         out.log_ints = arena.alloc<int>(want);

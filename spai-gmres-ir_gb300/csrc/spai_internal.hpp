@@ -6,10 +6,75 @@
 
 #include <cstddef>
 #include <cstdint>
+#include <cstdlib>
+#include <map>
+#include <mutex>
 #include <string>
+#include <utility>
 #include <vector>
 
 namespace spai {
+
+// Process-wide cache of the device blocks that destroyed arenas held, per device. A one-call solve
+// creates and destroys a handle every call, and the cudaMalloc / cudaFree of its workspaces
+// (cudaFree synchronises the device) cost milliseconds per call; later arenas take a cached block
+// of at least the requested size and at most twice it. A failed cudaMalloc empties the cache and
+// retries. SPAI_BLOCK_CACHE=0 turns the cache off.
+class BlockCache {
+  public:
+    // A cached block of `bytes` to 2 * `bytes` bytes (its size in *got), or nullptr.
+    void *take(size_t bytes, size_t *got) {
+        if (!enabled())
+            return nullptr;
+        int dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess)
+            return nullptr;
+        std::lock_guard<std::mutex> lock(mu_);
+        auto it = free_.lower_bound({dev, bytes});
+        if (it == free_.end() || it->first.first != dev || it->first.second > 2 * bytes)
+            return nullptr;
+        void *p = it->second;
+        *got = it->first.second;
+        free_.erase(it);
+        return p;
+    }
+    // p must be idle: no kernel or copy in flight uses it.
+    void give(void *p, size_t bytes) {
+        int dev = 0;
+        if (!enabled() || cudaGetDevice(&dev) != cudaSuccess) {
+            cudaFree(p);
+            return;
+        }
+        std::lock_guard<std::mutex> lock(mu_);
+        free_.insert({{dev, bytes}, p});
+    }
+    void release() {
+        std::lock_guard<std::mutex> lock(mu_);
+        int dev0 = 0;
+        cudaGetDevice(&dev0);
+        for (auto &kv : free_) {
+            cudaSetDevice(kv.first.first);
+            cudaFree(kv.second);
+        }
+        free_.clear();
+        cudaSetDevice(dev0);
+    }
+    static bool enabled() {
+        static const bool on = [] {
+            const char *e = std::getenv("SPAI_BLOCK_CACHE");
+            return !(e && std::atoi(e) == 0);
+        }();
+        return on;
+    }
+
+  private:
+    std::mutex mu_;
+    std::multimap<std::pair<int, size_t>, void *> free_;
+};
+inline BlockCache &block_cache() {
+    static BlockCache *c = new BlockCache(); // never destroyed: the driver frees device memory at exit
+    return *c;
+}
 
 // Device CSR with 32-bit indices (nnz < 2^31 is checked at upload).
 template <class T> struct DeviceCsr {
@@ -27,9 +92,15 @@ class DeviceArena {
     DeviceArena(const DeviceArena &) = delete;
     DeviceArena &operator=(const DeviceArena &) = delete;
     ~DeviceArena() {
+        bool any = false;
+        for (auto &s : slots_)
+            any |= s.ptr != nullptr;
+        if (!any)
+            return;
+        cudaDeviceSynchronize(); // the blocks are idle before others may take them
         for (auto &s : slots_)
             if (s.ptr)
-                cudaFree(s.ptr);
+                block_cache().give(s.ptr, s.bytes);
     }
     void reset() {
         next_ = 0;
@@ -41,11 +112,18 @@ class DeviceArena {
         Slot &s = slots_[next_++];
         if (s.bytes < bytes) {
             if (s.ptr)
-                SPAI_CUDA(cudaFree(s.ptr));
+                SPAI_CUDA(cudaFree(s.ptr)); // synchronises: the old block may still be in use
             s.ptr = nullptr;
             s.bytes = 0;
-            SPAI_CUDA(cudaMalloc(&s.ptr, bytes));
-            s.bytes = bytes;
+            size_t got = bytes;
+            void *p = block_cache().take(bytes, &got);
+            if (!p && cudaMalloc(&p, bytes) != cudaSuccess) {
+                cudaGetLastError();
+                block_cache().release();
+                SPAI_CUDA(cudaMalloc(&p, bytes));
+            }
+            s.ptr = p;
+            s.bytes = got;
         }
         return static_cast<U *>(s.ptr);
     }

@@ -315,9 +315,12 @@ class Handle:
                            pivot_ratio=float(vals[vo + 1]), coefficients=vals[vo + 2:vo + 2 + a].copy())
                 pos += 8 + a + b
             elif kind == 2:
-                rec = dict(candidates=body[:a].tolist(), selected=body[a:a + b].tolist(),
-                           mean_score=float(vals[vo]), scores=vals[vo + 1:vo + 1 + a].copy())
-                pos += 8 + a + c
+                rec = dict(candidates=body[:a].tolist(), mean_score=float(vals[vo]),
+                           scores=vals[vo + 1:vo + 1 + a].copy())
+                pos += 8 + a
+            elif kind == 3:
+                rec = dict(selected=body[:a].tolist())
+                pos += 8 + a
             else:
                 raise SpaiError(-1, f"corrupt fit log record kind {kind} at {pos}")
             recs.setdefault(k, []).append((tier, fit, kind, rec))

@@ -25,7 +25,7 @@ UNITS = {
     "mm_device.o": ("mm_device.cu", []),
 }
 HEADERS = ["common.cuh", "exact_math.cuh", "spai_internal.hpp", "krylov.cuh", "krylov_kernels.cuh",
-           "cgs_tiles.cuh", "adjoint.cuh", "sell.cuh", "mm_text.hpp", "cli_read.hpp"]
+           "cgs_tiles.cuh", "adjoint.cuh", "sell.cuh", "dia.cuh", "mm_text.hpp", "cli_read.hpp"]
 CLIS = {"gpu_fp64_ir": ("cli_main.cpp", "-DSOLVER_F64"), "gpu_fp32_ir": ("cli_main.cpp", "-DSOLVER_F32"),
         "gpu_mixed_ir": ("cli_main.cpp", "-DSOLVER_MIXED"), "gpu_diag_ir": ("diag_main.cpp", "")}
 

@@ -157,7 +157,7 @@ def _construction(h, status):
             fits.append({"J": f["J"], "I": f["I"], "coefficients": _vals(f["coefficients"]),
                          "candidates": f["candidates"] if scored else [],
                          "scores": _vals(f["scores"]) if scored else [],
-                         "selected": f["selected"] if scored else [],
+                         "selected": f.get("selected", []),
                          "residual": _hex(f["residual"]), "full_residual": _hex(f["residual"]),
                          "mean_score": _hex(f["mean_score"] if scored else 0.0),
                          "pivot_ratio": _hex(f["pivot_ratio"])})
