@@ -88,11 +88,16 @@ enum {
                                 candidate sets instead of the reference's sequential arithmetic
                                 (patterns may differ on near-tied scores; not bit-reproducible) */
     SPAI_FLAG_HISTORY = 4,   /* record the refinement history of the solve (spai_history) */
-    SPAI_FLAG_RESTART_AT_CAP = 8 /* an inner GMRES that reaches its cap with a verified candidate
+    SPAI_FLAG_RESTART_AT_CAP = 8, /* an inner GMRES that reaches its cap with a verified candidate
                                     that reduces the preconditioned residual (relative < 1) supplies
                                     the correction anyway: the refinement restarts GMRES from the new
                                     binary64 residual, i.e. restarted GMRES(innercap) inside IR
                                     (the reference stops with inner_failure; off by default) */
+    SPAI_FLAG_RIGHT_PRECONDITIONING = 16 /* inner GMRES on A P u = r with correction d = P u: the
+                                    form flexible GMRES takes with this solver's one fixed SPAI;
+                                    its estimate and acceptance test are relative to ||r||, the
+                                    unpreconditioned residual (the reference's inner solve is
+                                    left-preconditioned; off by default) */
 };
 
 /* Refinement history of one solve (IrResult::history / inner_history / update_applied and

@@ -41,14 +41,20 @@ __global__ void convert_kernel(long long count, const TS *src, TD *dst) {
 // row, values finite and nonzero. Offsets are clamped into [0, nnz] before use and a row whose
 // offsets decrease is skipped, so no read leaves the arrays whatever the input; *bad != 0 means
 // canonical_error (host) names the first violation.
+// bad[1] receives the longest row (the sparsity profile's max_row) of a valid matrix.
 __global__ void csr_offsets_kernel(long long n, long long nnz, const long long *rp64, int *rp32, int *bad) {
+    int longest = 0;
     for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i <= n;
          i += static_cast<long long>(gridDim.x) * blockDim.x) {
         const long long v = rp64[i];
         if (v < 0 || v > nnz || (i < n && rp64[i + 1] < v))
-            *bad = 1;
+            bad[0] = 1;
+        else if (i < n && rp64[i + 1] - v > longest)
+            longest = static_cast<int>(min(rp64[i + 1] - v, nnz));
         rp32[i] = static_cast<int>(v < 0 ? 0 : (v > nnz ? nnz : v));
     }
+    if (longest > 0)
+        atomicMax(bad + 1, longest);
 }
 __global__ void csr_entries_kernel(int n, const int *rp32, const long long *ci64, const double *val, int *ci32,
                                    int *bad) {
@@ -150,6 +156,7 @@ struct spai_handle_s {
     IrEngine<float, double> emix;
     IrEngine<float, float> e32;
     int engine_cap = -1;
+    bool engine_right = false; // the engine runs right-preconditioned GMRES
     // Adjoint solves A^T lambda = g: transposes of A and P built on first use after a build, and
     // engines in right-preconditioned mode over them.
     DeviceArena adj, adj_solve, conv;
@@ -235,19 +242,22 @@ void clear_report(spai_report *r) {
     r->forward_error = NAN;
 }
 
-void ensure_engine(spai_handle *h, int cap) {
-    if (h->engine_cap == cap)
+// Solve engine for `cap` inner steps; right: GMRES on A P d = rhs with x = P d (the form flexible
+// GMRES takes with one fixed preconditioner), else the reference's left-preconditioned P A.
+void ensure_engine(spai_handle *h, int cap, bool right = false) {
+    if (h->engine_cap == cap && h->engine_right == right)
         return;
     h->solve.reset();
     const int sms = h->sms;
     if (h->precision == SPAI_PREC_F64)
-        h->e64.setup(h->solve, h->a64, h->a64, h->s64.p, cap, sms);
+        h->e64.setup(h->solve, h->a64, h->a64, h->s64.p, cap, sms, right);
     else if (h->precision == SPAI_PREC_MIXED)
-        h->emix.setup(h->solve, h->a64, h->a32, h->s32.p, cap, sms);
+        h->emix.setup(h->solve, h->a64, h->a32, h->s32.p, cap, sms, right);
     else
-        h->e32.setup(h->solve, h->a32, h->a32, h->s32.p, cap, sms);
+        h->e32.setup(h->solve, h->a32, h->a32, h->s32.p, cap, sms, right);
     h->e64.prof = h->emix.prof = h->e32.prof = &h->prof;
     h->engine_cap = cap;
+    h->engine_right = right;
 }
 
 template <class E> void read_ctl(spai_handle *h, E &e, Ctl &c) {
@@ -385,7 +395,7 @@ int solve_device_impl(spai_handle *h, const double *d_b, double *d_x, const spai
         return SPAI_OK;
     }
     const int cap = o.innercap == 0 ? h->n : static_cast<int>(o.innercap);
-    ensure_engine(h, cap);
+    ensure_engine(h, cap, (o.flags & SPAI_FLAG_RIGHT_PRECONDITIONING) != 0);
     SolveSettings s = settings_for(h, o, cap);
     if (h->recording) { // record mode: host-driven loop, every step read back (binary64 handles)
         h->krec.clear();
@@ -478,23 +488,20 @@ int adjoint_device_impl(spai_handle *h, int nrhs, const double *d_x, const doubl
 namespace spai_api {
 // Host CSR -> device CSR in `dst` (64-bit indices narrowed on the device through the handle's
 // scratch arena), checked on the device for the canonical form on the way; stream-ordered. The
-// caller synchronises and, when *bad is set, reports canonical_error's message. `a` must pass
-// canonical_header_error.
+// caller synchronises and, when bad[0] is set, reports canonical_error's message; bad[1] is then
+// the longest row. `a` must pass canonical_header_error.
 DeviceCsr<double> upload_csr(spai_handle *h, DeviceArena &dst, const spai_csr *a, int *bad) {
     const int n = static_cast<int>(a->n), nnz = static_cast<int>(a->nnz);
     DeviceCsr<double> m;
     m.n = n;
     m.nnz = nnz;
-    int max_row = 0;
-    for (int64_t r = 0; r < a->n; ++r)
-        max_row = std::max<int>(max_row, static_cast<int>(a->row_offsets[r + 1] - a->row_offsets[r]));
-    m.max_row = max_row;
+    m.max_row = 0; // bad[1] after the caller's synchronisation
     m.rp = dst.alloc<int>(n + 1);
     m.ci = dst.alloc<int>(nnz > 0 ? nnz : 1);
     m.val = dst.alloc<double>(nnz > 0 ? nnz : 1);
     long long *tmp = h->scratch.alloc<long long>(std::max(n + 1, nnz));
     cudaStream_t st = h->stream;
-    SPAI_CUDA(cudaMemsetAsync(bad, 0, sizeof(int), st));
+    SPAI_CUDA(cudaMemsetAsync(bad, 0, 2 * sizeof(int), st));
     SPAI_CUDA(cudaMemcpyAsync(tmp, a->row_offsets, sizeof(long long) * (n + 1), cudaMemcpyHostToDevice, st));
     csr_offsets_kernel<<<grid_for(n + 1, 256, h->sms * 8), 256, 0, st>>>(n, nnz, tmp, m.rp, bad);
     SPAI_LAUNCH("csr_offsets_kernel");
@@ -616,25 +623,25 @@ int spai_create(const spai_csr *a, int32_t precision, int device, void *stream, 
     const int n = h->n, nnz = h->nnz;
     cudaStream_t st = h->stream;
     h->scratch.reset();
-    int *bad = h->scratch.alloc<int>(1);
+    int *bad = h->scratch.alloc<int>(2);
     h->a64 = upload_csr(h.get(), h->mat, a, bad);
     if (precision != SPAI_PREC_F64) {
         h->a32.n = n;
         h->a32.nnz = nnz;
-        h->a32.max_row = h->a64.max_row;
         h->a32.rp = h->a64.rp;
         h->a32.ci = h->a64.ci;
         h->a32.val = h->mat.alloc<float>(nnz);
         convert_kernel<float, double><<<grid_for(nnz, 256, h->sms * 8), 256, 0, st>>>(nnz, h->a64.val, h->a32.val);
         SPAI_LAUNCH("convert_kernel");
     }
-    int h_bad = 0;
-    SPAI_CUDA(cudaMemcpyAsync(&h_bad, bad, sizeof(int), cudaMemcpyDeviceToHost, st));
+    int h_bad[2] = {0, 0};
+    SPAI_CUDA(cudaMemcpyAsync(h_bad, bad, sizeof(h_bad), cudaMemcpyDeviceToHost, st));
     SPAI_CUDA(cudaStreamSynchronize(st));
-    if (h_bad) { // the host check names the first violation
+    if (h_bad[0]) { // the host check names the first violation
         const std::string full = canonical_error(a);
         return fail(SPAI_ERR_ARGUMENT, "spai_create: " + (full.empty() ? std::string("CSR is not canonical") : full));
     }
+    h->a64.max_row = h->a32.max_row = h_bad[1];
     *out = h.release();
     return SPAI_OK;
     API_END
@@ -1076,12 +1083,13 @@ int spai_set_preconditioner(spai_handle *h, const spai_csr *p) {
     h->adj_cap = -1;
     h->build.reset();
     h->scratch.reset();
-    int *bad = h->scratch.alloc<int>(1);
-    const DeviceCsr<double> p64 = upload_csr(h, h->build, p, bad);
-    int h_bad = 0;
-    SPAI_CUDA(cudaMemcpyAsync(&h_bad, bad, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    int *bad = h->scratch.alloc<int>(2);
+    DeviceCsr<double> p64 = upload_csr(h, h->build, p, bad);
+    int h_bad[2] = {0, 0};
+    SPAI_CUDA(cudaMemcpyAsync(h_bad, bad, sizeof(h_bad), cudaMemcpyDeviceToHost, h->stream));
     SPAI_CUDA(cudaStreamSynchronize(h->stream));
-    if (h_bad) {
+    p64.max_row = h_bad[1];
+    if (h_bad[0]) {
         const std::string full = canonical_error(p);
         return fail(SPAI_ERR_ARGUMENT, "spai_set_preconditioner: " + (full.empty() ? std::string("CSR is not canonical") : full));
     }

@@ -19,6 +19,7 @@ FLAG_NO_GRAPH = 1
 FLAG_FAST_SPAI = 2
 FLAG_HISTORY = 4
 FLAG_RESTART_AT_CAP = 8
+FLAG_RIGHT_PRECONDITIONING = 16
 FLAG_EXACT_SPAI = 0  # sequential, bit-reproducing SPAI (the default)
 
 SPAI_STATUS = ["success", "not_attempted", "invalid_input", "rank_deficient", "numerical_failure",
