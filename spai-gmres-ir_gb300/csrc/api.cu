@@ -23,12 +23,6 @@ int fail(int code, const std::string &msg) {
     return code;
 }
 
-// int64 host CSR -> int32 device CSR (upload once, convert on the device).
-__global__ void narrow_kernel(long long count, const long long *src, int *dst) {
-    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < count;
-         i += static_cast<long long>(gridDim.x) * blockDim.x)
-        dst[i] = static_cast<int>(src[i]);
-}
 template <class TD, class TS>
 __global__ void convert_kernel(long long count, const TS *src, TD *dst) {
     for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < count;

@@ -4,6 +4,7 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstddef>
 #include <cstdint>
 #include <cstdlib>
@@ -38,10 +39,9 @@ class BlockCache {
         free_.erase(it);
         return p;
     }
-    // p must be idle: no kernel or copy in flight uses it.
-    void give(void *p, size_t bytes) {
-        int dev = 0;
-        if (!enabled() || cudaGetDevice(&dev) != cudaSuccess) {
+    // p (allocated on device dev) must be idle: no kernel or copy in flight uses it.
+    void give(int dev, void *p, size_t bytes) {
+        if (!enabled()) {
             cudaFree(p);
             return;
         }
@@ -92,15 +92,24 @@ class DeviceArena {
     DeviceArena(const DeviceArena &) = delete;
     DeviceArena &operator=(const DeviceArena &) = delete;
     ~DeviceArena() {
-        bool any = false;
+        // Every device holding a block is synchronised first: the blocks are idle before other
+        // arenas may take them from the cache.
+        std::vector<int> devs;
         for (auto &s : slots_)
-            any |= s.ptr != nullptr;
-        if (!any)
+            if (s.ptr && std::find(devs.begin(), devs.end(), s.dev) == devs.end())
+                devs.push_back(s.dev);
+        if (devs.empty())
             return;
-        cudaDeviceSynchronize(); // the blocks are idle before others may take them
+        int dev0 = 0;
+        cudaGetDevice(&dev0);
+        for (int d : devs) {
+            cudaSetDevice(d);
+            cudaDeviceSynchronize();
+        }
+        cudaSetDevice(dev0);
         for (auto &s : slots_)
             if (s.ptr)
-                block_cache().give(s.ptr, s.bytes);
+                block_cache().give(s.dev, s.ptr, s.bytes);
     }
     void reset() {
         next_ = 0;
@@ -124,6 +133,7 @@ class DeviceArena {
             }
             s.ptr = p;
             s.bytes = got;
+            SPAI_CUDA(cudaGetDevice(&s.dev));
         }
         return static_cast<U *>(s.ptr);
     }
@@ -138,6 +148,7 @@ class DeviceArena {
     struct Slot {
         void *ptr = nullptr;
         size_t bytes = 0;
+        int dev = 0; // device the block belongs to
     };
     std::vector<Slot> slots_;
     size_t next_ = 0;
