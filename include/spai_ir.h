@@ -233,7 +233,8 @@ int spai_set_preconditioner(spai_handle *h, const spai_csr *p);
  * it, gmres.cpp:235-240, so results equal the unrecorded solve's up to the three-pass
  * orthogonalisation) and keeps what the reference's GmresResult and IrResult histories hold
  * (include/bspai/gmres.hpp:28-50, ir.hpp:36-56): every step's candidate, the basis, the
- * unrotated Hessenberg, every iterate and residual. Diagnostics for small systems; the records
+ * unrotated Hessenberg, every iterate and residual. Diagnostics for small systems: a recorded solve
+ * needs n * (innercap + 1) * (outercap + 1) below 2^28 (SPAI_ERR_ARGUMENT otherwise); the records
  * live in host memory of the handle until the next recorded solve. No reference counterpart
  * beyond those result structures (the reference's release snapshot prints them,
  * tests/release_cpu_snapshot.cpp:281-398). */

@@ -392,6 +392,9 @@ int solve_device_impl(spai_handle *h, const double *d_b, double *d_x, const spai
     ensure_engine(h, cap, (o.flags & SPAI_FLAG_RIGHT_PRECONDITIONING) != 0);
     SolveSettings s = settings_for(h, o, cap);
     if (h->recording) { // record mode: host-driven loop, every step read back (binary64 handles)
+        if (static_cast<double>(h->n) * (cap + 1) * (o.outercap + 1) > static_cast<double>(1 << 28))
+            return fail(SPAI_ERR_ARGUMENT, "record mode keeps every step's candidate in host memory: "
+                                           "n * (innercap + 1) * (outercap + 1) must stay below 2^28");
         h->krec.clear();
         s.record = &h->krec;
         s.history = true;
@@ -993,6 +996,9 @@ int spai_gmres(spai_handle *h, const double *rhs, double *x, double tau, int64_t
     s.tau = tau;
     s.accept_every = h->precision == SPAI_PREC_F32;
     if (h->recording) {
+        if (static_cast<double>(n) * (c + 1) > static_cast<double>(1 << 28))
+            return fail(SPAI_ERR_ARGUMENT, "record mode keeps every step's candidate in host memory: "
+                                           "n * (cap + 1) must stay below 2^28");
         h->krec.clear();
         s.record = &h->krec;
     }
