@@ -9,7 +9,9 @@ is not:
 * every fit history grows its pattern by its selection, and its shadow is the union of B's
   column patterns over J; the selection is the binary64 (score, index) order below the mean;
 * recorded GMRES solves satisfy P A V_m = V_{m+1} H_m, keep v_0..v_{m-1} orthonormal, and the
-  refinement's states satisfy r = b - A x and x_s = x_{s-1} + d_s.
+  refinement's states satisfy r = b - A x and x_s = x_{s-1} + d_s;
+* the device's fit histories and P equal the oracle's bit for bit, and its GMRES case matches
+  the oracle's solve.
 """
 import json
 import math
@@ -19,6 +21,8 @@ from fractions import Fraction
 
 import numpy as np
 import pytest
+
+from spai_ir import SPAI_STATUS
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 FIXTURE = os.path.join(HERE, "golden", "release_snapshot_gb300.txt")
@@ -176,3 +180,45 @@ def test_refinement_relations(items, case):
     assert len(ir["updates"]) == len(ir["inner_history"]) == ir["inner_attempts"]
     if ir["converged"]:
         assert _num(hist[-1]["diagnostics"]["nbe"]) <= 10 * 2.0 ** -53
+
+
+@pytest.mark.parametrize("case", ["spai_direct_full", "spai_gmres_ir", "spai_tie_growth", "spai_near_dependent"])
+def test_device_fit_histories_equal_the_oracle(items, case, built):
+    """The GB300's fit log in the fixture equals the oracle's fit histories bit for bit."""
+    import oracle as O
+
+    it = items[case]
+    a = it["A"]
+    system = (a["rows"], np.array(a["offsets"], np.int64), np.array(a["indices"], np.int64), _vec(a["values"]))
+    ref = O.Spai(system, _num(it["epsilon"]), it["alpha"], it["beta"], history=True)
+    cols = it["construction"]["columns"]
+    assert [c["status"] for c in cols] == [SPAI_STATUS[s] for s in ref.col_status]
+    for k, col in enumerate(cols):
+        assert len(col["history"]) == ref.fits[k]
+        for f, fit in enumerate(col["history"]):
+            r = ref.fit(k, f)
+            assert fit["J"] == list(r["pattern"]) and fit["I"] == list(r["shadow"])
+            assert list(_vec(fit["coefficients"])) == list(r["coefficients"])
+            assert _num(fit["residual"]) == r["residual"] and _num(fit["pivot_ratio"]) == r["pivot_ratio"]
+            assert fit["candidates"] == list(r["candidates"]) and fit["selected"] == list(r["selected"])
+            assert list(_vec(fit["scores"])) == list(r["scores"])
+            if fit["candidates"]:
+                assert _num(fit["mean_score"]) == r["mean_score"]
+    pd = _dense(it["construction"]["P"])
+    po = np.zeros_like(pd)
+    for i in range(ref.n):
+        po[i, ref.p_idx[ref.p_ptr[i]:ref.p_ptr[i + 1]]] = ref.p_val[ref.p_ptr[i]:ref.p_ptr[i + 1]]
+    assert np.array_equal(pd, po)
+
+
+def test_device_gmres_case_matches_the_oracle(items, built):
+    import oracle as O
+
+    it = items["gmres_identity_nonsymmetric"]
+    a, p = it["A"], it["fixed_P"]
+    sys_a = (a["rows"], np.array(a["offsets"], np.int64), np.array(a["indices"], np.int64), _vec(a["values"]))
+    sys_p = (p["rows"], np.array(p["offsets"], np.int64), np.array(p["indices"], np.int64), _vec(p["values"]))
+    x, rep = O.gmres(sys_a, sys_p, _vec(it["b"]), tol=1e-8)
+    g = it["gmres"]
+    assert rep["iterations"] == g["iterations"] and g["status"] == "success" and rep["status"] == 0
+    np.testing.assert_allclose(_vec(g["solution"]), x, rtol=1e-13, atol=1e-15)
